@@ -1,0 +1,313 @@
+// Divide on the GPU: min-hash grouping of the active supernodes
+// (Sweg::Divide, src/sweg.cpp:853-890, with SplitGroupByHashDims /
+// FallbackSplitGroup / SupernodeMinHash at src/sweg.cpp:754-851).
+//
+// The reference recursion sorts a range by (min-hash of dimension
+// dim_order[depth], rep) and recurses on equal-hash runs longer than
+// divide_max_group. The same order is produced breadth-first: every
+// unfinished segment (a run longer than divide_max_group) is already sorted by
+// rep (it is a run of equal hashes of the previous depth, tie-broken by rep),
+// so one stable segmented sort by the next hash per depth yields
+// (hash, rep) order inside each segment; equal-hash boundaries become new
+// segment heads. After divide_hash_dims depths the remaining long segments are
+// stably sorted by FallbackRank and cut into divide_max_group chunks. Groups
+// are the final segments in position order, exactly the reference's DFS order.
+//
+// Min-hash per supernode = min over member nodes v and their CSR neighbours u
+// of HashRank64(., dim, iter): one pass over the arcs whose source belongs to
+// a supernode still in an unfinished segment, warp-aggregated atomicMin per
+// supernode, plus one self term per node.
+
+#include <cub/device/device_scan.cuh>
+#include <cub/device/device_segmented_sort.cuh>
+
+#include <algorithm>
+#include <numeric>
+
+#include "engine.h"
+
+namespace beam {
+namespace {
+
+__global__ void ActiveFlagsKernel(const int* __restrict__ qsize, int n, int* __restrict__ flags) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) flags[i] = qsize[i] > 0 ? 1 : 0;
+}
+
+// order[scan[i]] = i for active reps; scan is exclusive.
+__global__ void ScatterActiveKernel(const int* __restrict__ qsize, const int* __restrict__ scan, int n,
+                                    int* __restrict__ order, int* __restrict__ head_flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && qsize[i] > 0) {
+    const int p = scan[i];
+    order[p] = i;
+    head_flag[p] = p == 0 ? 1 : 0;
+  }
+}
+
+// Segment descriptors from head flags: segid (inclusive scan - 1) per
+// position, start per segment.
+__global__ void SegStartsKernel(const int* __restrict__ head_flag, const int* __restrict__ incl, int count,
+                                int* __restrict__ seg_start) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < count && head_flag[p]) seg_start[incl[p] - 1] = p;
+}
+
+__global__ void SegLenKernel(const int* __restrict__ seg_start, int segs, int count, int max_group,
+                             int* __restrict__ seg_len, int* __restrict__ unf_flag, int* __restrict__ unf_len) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < segs) {
+    const int end = s + 1 < segs ? seg_start[s + 1] : count;
+    const int len = end - seg_start[s];
+    seg_len[s] = len;
+    const int unf = len > max_group ? 1 : 0;
+    unf_flag[s] = unf;
+    unf_len[s] = unf ? len : 0;
+  }
+}
+
+// Compact the items of unfinished segments: pos_map[k] = position,
+// item_seg[k] = compact segment index; segment begin/end in compact space.
+__global__ void CompactItemsKernel(const int* __restrict__ incl, const int* __restrict__ seg_start,
+                                   const int* __restrict__ seg_len, const int* __restrict__ unf_flag,
+                                   const int* __restrict__ unf_idx, const int* __restrict__ unf_off, int count,
+                                   int* __restrict__ pos_map, int* __restrict__ item_seg,
+                                   int* __restrict__ ubeg, int* __restrict__ uend) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= count) return;
+  const int s = incl[p] - 1;
+  if (!unf_flag[s]) return;
+  const int r = p - seg_start[s];
+  const int k = unf_off[s] + r;
+  pos_map[k] = p;
+  item_seg[k] = unf_idx[s];
+  if (r == 0) {
+    ubeg[unf_idx[s]] = unf_off[s];
+    uend[unf_idx[s]] = unf_off[s] + seg_len[s];
+  }
+}
+
+__global__ void MarkNeedKernel(const int* __restrict__ order, const int* __restrict__ pos_map, int items,
+                               int* __restrict__ need, int stamp, unsigned long long* __restrict__ hash) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < items) {
+    const int rep = order[pos_map[k]];
+    need[rep] = stamp;
+    hash[rep] = ~0ull;
+  }
+}
+
+// One thread per arc (plus one per node for the node's own rank). Lanes of a
+// warp whose sources share a supernode combine their minima before a single
+// atomicMin; arcs are grouped by source, so this removes most atomics.
+__global__ void MinHashKernel(const int* __restrict__ arc_src, const int* __restrict__ col,
+                              const int* __restrict__ label, const int* __restrict__ need, long long arcs, int n,
+                              int stamp, uint64_t base, unsigned long long* __restrict__ hash) {
+  const long long total = arcs + n;
+  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
+  for (long long t0 = static_cast<long long>(blockIdx.x) * blockDim.x; t0 < total; t0 += stride) {
+    const long long t = t0 + threadIdx.x;
+    int rep = -1;
+    unsigned long long h = ~0ull;
+    if (t < total) {
+      const int node = t < arcs ? arc_src[t] : static_cast<int>(t - arcs);
+      const int r = label[node];
+      if (need[r] == stamp) {
+        rep = r;
+        h = HashRankWithBase(base, t < arcs ? col[t] : node);
+      }
+    }
+    // exact minimum over the lanes holding the same supernode: high words
+    // first, then low words among the lanes that hold the minimal high word
+    const unsigned mask = __match_any_sync(0xffffffffu, rep);
+    const unsigned hi = static_cast<unsigned>(h >> 32);
+    const unsigned lo = static_cast<unsigned>(h & 0xffffffffu);
+    const unsigned mhi = __reduce_min_sync(mask, hi);
+    const unsigned mlo = __reduce_min_sync(mask, hi == mhi ? lo : 0xffffffffu);
+    const unsigned long long g = (static_cast<unsigned long long>(mhi) << 32) | mlo;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    if (rep >= 0 && lane == leader) atomicMin(&hash[rep], g);
+  }
+}
+
+__global__ void GatherKeysKernel(const int* __restrict__ order, const int* __restrict__ pos_map, int items,
+                                 const unsigned long long* __restrict__ hash, int fallback, uint64_t seed,
+                                 int iter, unsigned long long* __restrict__ keys, int* __restrict__ vals) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < items) {
+    const int rep = order[pos_map[k]];
+    keys[k] = fallback ? FallbackRank(seed, rep, iter) : hash[rep];
+    vals[k] = rep;
+  }
+}
+
+__global__ void ScatterSortedKernel(const int* __restrict__ pos_map, const int* __restrict__ item_seg,
+                                    const int* __restrict__ ubeg, int items,
+                                    const unsigned long long* __restrict__ keys, const int* __restrict__ vals,
+                                    int fallback, int max_group, int* __restrict__ order,
+                                    int* __restrict__ head_flag) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= items) return;
+  const int p = pos_map[k];
+  order[p] = vals[k];
+  const int r = k - ubeg[item_seg[k]];
+  if (r > 0) {
+    const bool head = fallback ? (r % max_group) == 0 : keys[k] != keys[k - 1];
+    if (head) head_flag[p] = 1;
+  }
+}
+
+__global__ void GroupInfoKernel(const int* __restrict__ order, const int* __restrict__ incl,
+                                const int* __restrict__ seg_start, const int* __restrict__ seg_len, int count,
+                                int* __restrict__ group_of, int* __restrict__ idx_in_group,
+                                unsigned long long* __restrict__ stats) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= count) return;
+  const int s = incl[p] - 1;
+  const int rep = order[p];
+  group_of[rep] = s;
+  idx_in_group[rep] = p - seg_start[s];
+  if (p == seg_start[s]) atomicMax(&stats[kStDivideMaxGroup], static_cast<unsigned long long>(seg_len[s]));
+}
+
+inline int Blocks(long long items, int threads) {
+  return static_cast<int>((items + threads - 1) / threads);
+}
+
+}  // namespace
+
+void Engine::Divide(int iter) {
+  const int n = n_;
+  const int T = 256;
+  cudaStream_t s = stream_;
+  // scratch arrays: d_counts_ holds [flags | scan | seg_len | unf_flag | unf_len | unf_idx | unf_off | ubeg | uend]
+  d_counts_.ensure(static_cast<size_t>(n) * 9 + 64);
+  int* flags = d_counts_.p;
+  int* scan = flags + n;
+  int* seg_len = scan + n;
+  int* unf_flag = seg_len + n;
+  int* unf_len = unf_flag + n;
+  int* unf_idx = unf_len + n;
+  int* unf_off = unf_idx + n;
+  int* ubeg = unf_off + n;
+  int* uend = ubeg + n;
+  int* seg_start = d_seg_beg_.p;
+  int* item_seg = d_seg_end_.p;
+
+  auto scan_excl = [&](const int* in, int* out, int items) {
+    size_t bytes = 0;
+    CheckCuda(cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, items, s), "cub scan size");
+    d_cub_tmp_.ensure(bytes);
+    CheckCuda(cub::DeviceScan::ExclusiveSum(d_cub_tmp_.p, bytes, in, out, items, s), "cub exclusive scan");
+  };
+  auto scan_incl = [&](const int* in, int* out, int items) {
+    size_t bytes = 0;
+    CheckCuda(cub::DeviceScan::InclusiveSum(nullptr, bytes, in, out, items, s), "cub scan size");
+    d_cub_tmp_.ensure(bytes);
+    CheckCuda(cub::DeviceScan::InclusiveSum(d_cub_tmp_.p, bytes, in, out, items, s), "cub inclusive scan");
+  };
+  auto fetch2 = [&](const int* a, const int* b, int* ha, int* hb) {
+    CheckCuda(cudaMemcpyAsync(h_pin_.p, a, sizeof(int), cudaMemcpyDeviceToHost, s), "d2h");
+    CheckCuda(cudaMemcpyAsync(reinterpret_cast<int*>(h_pin_.p) + 1, b, sizeof(int), cudaMemcpyDeviceToHost, s),
+              "d2h");
+    CheckCuda(cudaStreamSynchronize(s), "sync");
+    *ha = reinterpret_cast<int*>(h_pin_.p)[0];
+    *hb = reinterpret_cast<int*>(h_pin_.p)[1];
+  };
+
+  // Active supernodes in ascending id order.
+  ActiveFlagsKernel<<<Blocks(n, T), T, 0, s>>>(d_qsize_.p, n, flags);
+  scan_excl(flags, scan, n);
+  CheckCuda(cudaMemsetAsync(d_head_flag_.p, 0, sizeof(int) * static_cast<size_t>(n), s), "memset");
+  ScatterActiveKernel<<<Blocks(n, T), T, 0, s>>>(d_qsize_.p, scan, n, d_order_.p, d_head_flag_.p);
+  int last_scan = 0, last_flag = 0;
+  fetch2(scan + n - 1, flags + n - 1, &last_scan, &last_flag);
+  const int count = last_scan + last_flag;
+  n_active_ = count;
+
+  // dim_order: dims stable-sorted by (DimRank, dim)
+  std::vector<int> dim_order(static_cast<size_t>(cfg_.divide_hash_dims));
+  std::iota(dim_order.begin(), dim_order.end(), 0);
+  std::stable_sort(dim_order.begin(), dim_order.end(), [&](int a, int b) {
+    const uint64_t ra = DimRank(cfg_.seed, a, iter);
+    const uint64_t rb = DimRank(cfg_.seed, b, iter);
+    if (ra != rb) return ra < rb;
+    return a < b;
+  });
+
+  int segs = 0;
+  if (count > 0) {
+    for (int depth = 0; depth <= cfg_.divide_hash_dims; ++depth) {
+      const bool fallback = depth == cfg_.divide_hash_dims;
+      scan_incl(d_head_flag_.p, scan, count);
+      SegStartsKernel<<<Blocks(count, T), T, 0, s>>>(d_head_flag_.p, scan, count, seg_start);
+      int seg_total = 0, dummy = 0;
+      fetch2(scan + count - 1, scan + count - 1, &seg_total, &dummy);
+      segs = seg_total;
+      SegLenKernel<<<Blocks(segs, T), T, 0, s>>>(seg_start, segs, count, cfg_.divide_max_group, seg_len, unf_flag,
+                                                 unf_len);
+      scan_excl(unf_flag, unf_idx, segs);
+      scan_excl(unf_len, unf_off, segs);
+      int nu_last = 0, nu_flag = 0;
+      fetch2(unf_idx + segs - 1, unf_flag + segs - 1, &nu_last, &nu_flag);
+      const int nu = nu_last + nu_flag;
+      if (nu == 0) break;
+      int items_last = 0, items_len = 0;
+      fetch2(unf_off + segs - 1, unf_len + segs - 1, &items_last, &items_len);
+      const int items = items_last + items_len;
+      CompactItemsKernel<<<Blocks(count, T), T, 0, s>>>(scan, seg_start, seg_len, unf_flag, unf_idx, unf_off, count,
+                                                        d_pos_map_.p, item_seg, ubeg, uend);
+      if (fallback) {
+        hstats_.divide_fallback_splits += static_cast<uint64_t>(nu);
+      } else {
+        ++need_stamp_;
+        MarkNeedKernel<<<Blocks(items, T), T, 0, s>>>(d_order_.p, d_pos_map_.p, items, d_need_.p, need_stamp_,
+                                                      d_hash_.p);
+        const uint64_t base = HashRankBase(cfg_.seed, dim_order[static_cast<size_t>(depth)], iter);
+        BeginTimed(kTimeDivide);
+        MinHashKernel<<<152 * 8, 256, 0, s>>>(d_arc_src_.p, d_col_.p, d_label_.p, d_need_.p, arcs_, n,
+                                              need_stamp_, base, d_hash_.p);
+        EndTimed(kTimeDivide);
+      }
+      GatherKeysKernel<<<Blocks(items, T), T, 0, s>>>(d_order_.p, d_pos_map_.p, items, d_hash_.p, fallback ? 1 : 0,
+                                                      cfg_.seed, iter, d_keys_.p, d_vals_.p);
+      size_t bytes = 0;
+      CheckCuda(cub::DeviceSegmentedSort::StableSortPairs(nullptr, bytes, d_keys_.p, d_keys_alt_.p, d_vals_.p,
+                                                          d_vals_alt_.p, items, nu, ubeg, uend, s),
+                "cub segmented sort size");
+      d_cub_tmp_.ensure(bytes);
+      CheckCuda(cub::DeviceSegmentedSort::StableSortPairs(d_cub_tmp_.p, bytes, d_keys_.p, d_keys_alt_.p, d_vals_.p,
+                                                          d_vals_alt_.p, items, nu, ubeg, uend, s),
+                "cub segmented sort");
+      ScatterSortedKernel<<<Blocks(items, T), T, 0, s>>>(d_pos_map_.p, item_seg, ubeg, items, d_keys_alt_.p,
+                                                         d_vals_alt_.p, fallback ? 1 : 0, cfg_.divide_max_group,
+                                                         d_order_.p, d_head_flag_.p);
+    }
+    // final segments are the groups
+    scan_incl(d_head_flag_.p, scan, count);
+    SegStartsKernel<<<Blocks(count, T), T, 0, s>>>(d_head_flag_.p, scan, count, seg_start);
+    int seg_total = 0, dummy = 0;
+    fetch2(scan + count - 1, scan + count - 1, &seg_total, &dummy);
+    segs = seg_total;
+    SegLenKernel<<<Blocks(segs, T), T, 0, s>>>(seg_start, segs, count, cfg_.divide_max_group, seg_len, unf_flag,
+                                               unf_len);
+    GroupInfoKernel<<<Blocks(count, T), T, 0, s>>>(d_order_.p, scan, seg_start, seg_len, count, d_group_of_.p,
+                                                   d_idx_in_group_.p, d_stats_.p);
+    CheckCuda(cudaMemcpyAsync(d_gstart_.p, seg_start, sizeof(int) * static_cast<size_t>(segs),
+                              cudaMemcpyDeviceToDevice, s), "copy gstart");
+    CheckCuda(cudaMemcpyAsync(d_glen_.p, seg_len, sizeof(int) * static_cast<size_t>(segs),
+                              cudaMemcpyDeviceToDevice, s), "copy glen");
+  }
+  n_groups_ = segs;
+  h_glen_.resize(static_cast<size_t>(segs));
+  if (segs > 0) {
+    CheckCuda(cudaMemcpyAsync(h_glen_.data(), d_glen_.p, sizeof(int) * static_cast<size_t>(segs),
+                              cudaMemcpyDeviceToHost, s), "d2h glen");
+  }
+  CheckCuda(cudaStreamSynchronize(s), "divide sync");
+  hstats_.groups_last = static_cast<uint64_t>(segs);
+  hstats_.active_last = static_cast<uint64_t>(count);
+}
+
+}  // namespace beam

@@ -1,0 +1,208 @@
+// Host runtime of the GB300 merge loop: owns the device-resident graph,
+// quotient graph, partition lists and per-block scratch, and sequences the
+// kernels of Sweg::Run (src/sweg.cpp:651-709) on one CUDA stream.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace beam {
+
+struct EngineConfig {
+  int top_k = 16;
+  int group_batch_size = 64;
+  int divide_hash_dims = 16;
+  int divide_max_group = 512;
+  bool ea_use_threshold = true;
+  uint64_t seed = 1;
+  int device = 0;
+};
+
+// Largest group the kernels accept (bounded by the packed select keys and
+// the per-group pair tables); the reference default is 512.
+constexpr int kMaxGroup = 1024;
+// Persistent grid of the row-update kernel (two CTAs per SM of a GB300).
+constexpr int kRowsGrid = 2 * 152;
+
+void CheckCuda(cudaError_t status, const char* what);
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  void ensure(size_t count) {
+    if (count <= n) return;
+    release();
+    const size_t bytes = (count ? count : 1) * sizeof(T);
+    CheckCuda(cudaMalloc(reinterpret_cast<void**>(&p), bytes), "cudaMalloc");
+    n = count;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+template <typename T>
+struct PinnedBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  void ensure(size_t count) {
+    if (count <= n) return;
+    release();
+    CheckCuda(cudaMallocHost(reinterpret_cast<void**>(&p), (count ? count : 1) * sizeof(T)), "cudaMallocHost");
+    n = count;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+// Per-block control words, reset before every 64-group block.
+struct BlockCtl {
+  unsigned int acc_cnt;     // accepted merges in the block
+  unsigned int aff_cnt;     // neighbour rows to rewrite
+  unsigned long long scratch_top;  // bump pointer into the block scratch (bytes)
+};
+
+struct HostStats {
+  double runtime_run_ms = 0, runtime_divide_ms = 0, runtime_merge_ms = 0;
+  double merge_prepare_ms = 0, merge_score_ms = 0, merge_select_ms = 0, merge_update_ms = 0;
+  uint64_t iterations = 0, blocks = 0, groups_last = 0, active_last = 0;
+  uint64_t compactions = 0;
+  uint64_t divide_fallback_splits = 0;
+};
+
+// Timing of one kernel class with CUDA events on the engine stream.
+enum TimedKernel : int { kTimeNone = 0, kTimeScore = 1, kTimePrepare = 2, kTimeUpdate = 3, kTimeDivide = 4 };
+
+class Engine {
+ public:
+  Engine(int n, int64_t arcs, const int64_t* row_ptr, const int32_t* col_idx, const EngineConfig& cfg);
+  ~Engine();
+  Engine(const Engine&) = delete;
+  Engine& operator=(const Engine&) = delete;
+
+  // Singleton partition rebuilt from the resident CSR (QuotientGraph::Initialize).
+  void Reset();
+  // Sweg::Run / Divide / Merge.
+  void Run(int iterations);
+  void Divide(int iter);
+  void Merge(int iter, int total_iterations);
+
+  // Scoring service: ExactMergeGainPersistent for arbitrary pairs of active reps.
+  void ScorePairs(const int32_t* rep_a, const int32_t* rep_b, int64_t count, int64_t* gain, int64_t* before);
+  // EA-proxy candidate generation for one explicit group of active reps.
+  int64_t PrepareGroup(const int32_t* q, int g, int32_t* a_idx, int32_t* b_idx, int64_t cap);
+  // Applies endpoint-disjoint merges (keep, remove) as one commit batch.
+  void MergePairs(const int32_t* keep, const int32_t* remove, int64_t count);
+
+  // Views of the state (host copies).
+  void Partition(int32_t* labels, int32_t* head, int32_t* next);
+  void Groups(int32_t* order, int32_t* starts, int32_t* lengths);
+  int64_t ExportRow(int rep, int32_t* nb, int64_t* cnt, int64_t cap, int64_t* size, int64_t* internal);
+  void DeviceStats(uint64_t* out, int count);
+  int64_t QuotientNnz();
+  const HostStats& host_stats() const { return hstats_; }
+  int64_t active_count() const { return n_active_; }
+  int64_t group_count() const { return n_groups_; }
+  int n() const { return n_; }
+  int64_t arcs() const { return arcs_; }
+  const EngineConfig& config() const { return cfg_; }
+  cudaStream_t stream() const { return stream_; }
+
+  // Kernel timing for the roofline: events around every launch of one kernel class.
+  void SetTimedKernel(int which);
+  double TimedKernelMs();
+  int64_t TimedKernelLaunches() const { return timed_launches_; }
+  void Synchronize();
+
+ private:
+  void CheckError();
+  void InitQuotient();
+  void EnsurePoolRoom();
+  void CompactPool();
+  void RunBlock(int64_t g0, int64_t g1, int64_t max_cap, double threshold);
+  void PrepareIterationBuffers();
+  void BeginTimed(int which);
+  void EndTimed(int which);
+  void ConfigureKernels();
+  QuotientView View();
+  void LaunchCommit(int64_t g0, int nbg, bool check_gain);
+
+  int n_;
+  int64_t arcs_;
+  EngineConfig cfg_;
+  cudaStream_t stream_ = nullptr;
+
+  // graph
+  DevBuf<long long> d_rowptr_;
+  DevBuf<int> d_col_;
+  DevBuf<int> d_arc_src_;
+
+  // quotient graph
+  DevBuf<Entry> d_pool_[2];
+  int cur_pool_ = 0;
+  size_t pool_cap_ = 0;
+  DevBuf<unsigned long long> d_pool_top_;
+  DevBuf<long long> d_qoff_;
+  DevBuf<int> d_qlen_;
+  DevBuf<int> d_qcap_;
+  DevBuf<int> d_qsize_;
+  DevBuf<long long> d_qint_;
+
+  // partition
+  DevBuf<int> d_label_, d_head_, d_next_, d_tail_, d_fwd_;
+  DevBuf<int> d_stamp_, d_partner_, d_claim_;
+
+  // divide
+  DevBuf<int> d_order_, d_order_alt_, d_head_flag_;
+  DevBuf<unsigned long long> d_hash_, d_keys_, d_keys_alt_;
+  DevBuf<int> d_vals_, d_vals_alt_;
+  DevBuf<int> d_need_, d_seg_beg_, d_seg_end_, d_pos_map_;
+  DevBuf<int> d_gstart_, d_glen_, d_group_of_, d_idx_in_group_;
+  DevBuf<int> d_counts_;
+  DevBuf<unsigned char> d_cub_tmp_;
+  int need_stamp_ = 0;
+
+  // per-iteration merge buffers
+  DevBuf<long long> d_cand_off_, d_sel_off_, d_mat_off_;
+  DevBuf<int2> d_cand_;
+  DevBuf<longlong2> d_res_;
+  DevBuf<int> d_cand_cnt_;
+  DevBuf<int> d_sel_keep_, d_sel_rem_;
+  DevBuf<long long> d_sel_gain_;
+  DevBuf<unsigned char> d_sel_ok_;
+  DevBuf<int> d_sel_cnt_;
+  DevBuf<unsigned char> d_mat_;
+  DevBuf<unsigned char> d_scratch_;
+  DevBuf<int> d_acc_keep_, d_acc_rem_, d_aff_;
+  DevBuf<BlockCtl> d_ctl_;
+  DevBuf<unsigned long long> d_stats_;
+  DevBuf<DevError> d_err_;
+  std::vector<int> h_glen_;
+  std::vector<long long> h_cand_off_, h_sel_off_, h_mat_off_;
+  PinnedBuf<long long> h_pin_;
+  int block_stamp_ = 0;
+  int64_t n_active_ = 0;
+  int64_t n_groups_ = 0;
+  HostStats hstats_;
+
+  // kernel timing
+  int timed_kind_ = kTimeNone;
+  std::vector<cudaEvent_t> ev_pool_;
+  size_t ev_used_ = 0;
+  int64_t timed_launches_ = 0;
+  double timed_ms_accum_ = 0.0;
+};
+
+}  // namespace beam

@@ -1,0 +1,1373 @@
+// Merge on the GPU: the blocked EA merge loop (Sweg::Merge, blocked mode,
+// src/sweg.cpp:953-1145) for one 64-group block at a time.
+//
+//   PrepareKernel   EA-proxy candidates per group (src/sweg.cpp:1598-1727,1800-1999)
+//   ScoreKernel     exact merge gain per candidate pair
+//                   (QuotientGraph::ExactMergeGainPersistentImpl, src/quotient_graph.cpp:340-462)
+//   SelectKernel    reciprocal threshold filter + g0 greedy selection
+//                   (src/sweg.cpp:2146-2186, 2188-2281)
+//   ValidateKernel  commit-time exact gain against the block-start state
+//                   (CommitSelectedPairs, src/sweg.cpp:2683-2719)
+//   ApplyKernel     Update_S bookkeeping: sizes, internal counts, member lists
+//                   (src/sweg.cpp:2977-3015, src/quotient_graph.cpp:628-648)
+//   RowsKernel      quotient rows after the block's merges: keep rows rebuilt
+//                   from keep+remove, neighbour rows of removed supernodes
+//                   rewritten in place (src/quotient_graph.cpp:651-719)
+//
+// The reference validates every selected pair of a block before applying any
+// of them (Update_S runs after the validation loop), and the pairs of a block
+// are endpoint-disjoint, so the block's merges are applied as one batch; the
+// resulting rows are the canonical sorted, count-summed rows, identical to
+// the reference's sequential incremental updates.
+
+#include <cub/block/block_scan.cuh>
+
+#include <algorithm>
+
+#include "engine.h"
+
+namespace beam {
+namespace {
+
+constexpr int kPrepThreads = 256;
+constexpr int kSmemEntries = 2048;   // bucket entries held in shared memory
+constexpr int kSmemHeads = 4096;     // bucket hash heads in shared memory
+constexpr int kScoreThreads = 256;
+constexpr int kPairsPerScoreCta = 64;
+constexpr int kSelectThreads = 512;
+constexpr int kSelectSmemKeys = 8192;
+constexpr int kRowsThreads = 256;
+constexpr int kRowSmem = 2048;       // staged row entries in shared memory
+constexpr int kKeyIdxBits = 10;      // a_idx, b_idx < kMaxGroup
+constexpr long long kKeyGainMax = (1ll << (64 - 2 * kKeyIdxBits)) - 1;
+
+__device__ __forceinline__ unsigned long long* ScratchAlloc(unsigned char* base, unsigned long long cap,
+                                                           BlockCtl* ctl, unsigned long long bytes,
+                                                           DevError* err) {
+  bytes = (bytes + 255) & ~255ull;
+  const unsigned long long at = atomicAdd(&ctl->scratch_top, bytes);
+  if (at + bytes > cap) {
+    RaiseError(err, kErrScratch, static_cast<int>(bytes >> 20), static_cast<int>(cap >> 20), 0);
+    return nullptr;
+  }
+  return reinterpret_cast<unsigned long long*>(base + at);
+}
+
+// ------------------------------------------------------------ exact gain
+
+struct GainWork {
+  long long raw_a, raw_b, uni, ovl;
+};
+
+// Warp-cooperative ExactMergeGainPersistentImpl: lanes walk row a and look
+// each neighbour up in row b (shared neighbours give two before-terms), then
+// walk row b and keep the neighbours row a lacks; e(a,b) is read from both
+// rows and must agree. Every term is exact int64.
+__device__ void WarpExactGain(const QuotientView& Q, int a, int b, long long* gain_out, long long* before_out,
+                              GainWork* work, DevError* err) {
+  const int lane = threadIdx.x & 31;
+  const long long sa = Q.size[a];
+  const long long sb = Q.size[b];
+  const long long sw = sa + sb;
+  const Entry* ra = Q.ent + Q.off[a];
+  const Entry* rb = Q.ent + Q.off[b];
+  const int la = Q.len[a];
+  const int lb = Q.len[b];
+  long long before = 0, after = 0, eab_a = 0, eab_b = 0;
+  int uni = 0, ovl = 0, bad = 0;
+  for (int i = lane; i < la; i += 32) {
+    const Entry e = ra[i];
+    const int x = EntNb(e);
+    const long long ea = EntCnt(e);
+    if (x == b) {
+      eab_a = ea;
+      continue;
+    }
+    const long long eb = RowLookup(rb, lb, x);
+    const long long sx = Q.size[x];
+    if (eb != 0) {
+      before += BlockCost(sa, sx, ea, false, bad) + BlockCost(sb, sx, eb, false, bad);
+      ++ovl;
+    } else {
+      before += BlockCost(sa, sx, ea, false, bad);
+    }
+    after += BlockCost(sw, sx, ea + eb, false, bad);
+    ++uni;
+  }
+  for (int j = lane; j < lb; j += 32) {
+    const Entry e = rb[j];
+    const int x = EntNb(e);
+    const long long eb = EntCnt(e);
+    if (x == a) {
+      eab_b = eb;
+      continue;
+    }
+    if (RowLookup(ra, la, x) != 0) continue;
+    const long long sx = Q.size[x];
+    before += BlockCost(sb, sx, eb, false, bad);
+    after += BlockCost(sw, sx, eb, false, bad);
+    ++uni;
+  }
+  before = WarpSum(before);
+  after = WarpSum(after);
+  eab_a = WarpMax(eab_a);
+  eab_b = WarpMax(eab_b);
+  uni = WarpSumInt(uni);
+  ovl = WarpSumInt(ovl);
+  bad = __any_sync(0xffffffffu, bad);
+  if (eab_a != eab_b) {
+    if (lane == 0) RaiseError(err, kErrAsymmetric, a, b, 0);
+  }
+  const long long ia = Q.internal[a];
+  const long long ib = Q.internal[b];
+  before += BlockCost(sa, sa, ia, true, bad) + BlockCost(sb, sb, ib, true, bad) + BlockCost(sa, sb, eab_a, false, bad);
+  after += BlockCost(sw, sw, ia + ib + eab_a, true, bad);
+  if (bad && lane == 0) RaiseError(err, kErrBlockCost, a, b, 0);
+  *gain_out = before - after;
+  *before_out = before;
+  if (work) {
+    work->raw_a += la;
+    work->raw_b += lb;
+    work->uni += uni;
+    work->ovl += ovl;
+  }
+}
+
+// ------------------------------------------------------------ prepare
+
+struct PrepareParams {
+  QuotientView Q;
+  const int* order;
+  const int* gstart;
+  const int* glen;
+  const int* group_of;
+  const int* idx_in_group;
+  int g0;
+  const long long* cand_off;
+  int2* cand;
+  int* cand_cnt;
+  const long long* mat_off;
+  unsigned char* mat;
+  unsigned char* scratch;
+  unsigned long long scratch_cap;
+  BlockCtl* ctl;
+  int top_k;
+  unsigned long long* stats;
+  DevError* err;
+};
+
+struct RankKey {
+  double ratio;
+  long long pg;
+  int lo, hi, j;
+};
+
+// ranked_better (src/sweg.cpp:1926-1938): ratio desc, proxy gain desc,
+// rep_lo asc, rep_hi asc.
+__device__ __forceinline__ bool Better(const RankKey& x, const RankKey& y) {
+  if (x.ratio != y.ratio) return x.ratio > y.ratio;
+  if (x.pg != y.pg) return x.pg > y.pg;
+  if (x.lo != y.lo) return x.lo < y.lo;
+  return x.hi < y.hi;
+}
+
+__device__ __forceinline__ unsigned BucketHash(int t, unsigned mask) {
+  return (static_cast<unsigned>(t) * 0x9E3779B1u) >> 7 & mask;
+}
+
+struct PrepSmem {
+  int q[kMaxGroup];
+  int sz[kMaxGroup];
+  int len[kMaxGroup];
+  long long off[kMaxGroup];
+  long long old[kMaxGroup];
+  int eoff[kMaxGroup + 1];
+  int heads[kSmemHeads];
+  int et[kSmemEntries];
+  int ei[kSmemEntries];
+  unsigned ee[kSmemEntries];
+  int enx[kSmemEntries];
+  unsigned long long examined;
+  int total;
+};
+
+__global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PrepSmem& S = *reinterpret_cast<PrepSmem*>(smem_raw);
+  using BlockScan = cub::BlockScan<int, kPrepThreads>;
+  __shared__ typename BlockScan::TempStorage scan_tmp;
+  __shared__ int carry;
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  const int nwarps = kPrepThreads / 32;
+  const int gid = P.g0 + blockIdx.x;
+  const int g = P.glen[gid];
+  if (g < 2) {
+    if (tid == 0) P.cand_cnt[gid] = 0;
+    return;
+  }
+  if (g > kMaxGroup) {
+    if (tid == 0) {
+      RaiseError(P.err, kErrGroupTooLarge, gid, g, 0);
+      P.cand_cnt[gid] = 0;
+    }
+    return;
+  }
+  const QuotientView& Q = P.Q;
+  const int start = P.gstart[gid];
+  for (int i = tid; i < g; i += kPrepThreads) {
+    const int rep = P.order[start + i];
+    S.q[i] = rep;
+    S.sz[i] = Q.size[rep];
+    S.len[i] = Q.len[rep];
+    S.off[i] = Q.off[rep];
+  }
+  if (tid == 0) {
+    S.examined = 0;
+    carry = 0;
+  }
+  __syncthreads();
+  // exclusive scan of row lengths -> entry offsets
+  for (int base = 0; base < g; base += kPrepThreads) {
+    const int i = base + tid;
+    const int v = i < g ? S.len[i] : 0;
+    int ex = 0, agg = 0;
+    BlockScan(scan_tmp).ExclusiveSum(v, ex, agg);
+    if (i < g) S.eoff[i] = carry + ex;
+    __syncthreads();
+    if (tid == 0) carry += agg;
+    __syncthreads();
+  }
+  const int E = carry;
+  if (tid == 0) S.eoff[g] = E;
+  // bucket table: shared memory when it fits, block scratch otherwise
+  int* heads = S.heads;
+  int* et = S.et;
+  int* ei = S.ei;
+  unsigned* ee = S.ee;
+  int* enx = S.enx;
+  unsigned hmask = kSmemHeads - 1;
+  __shared__ unsigned long long* big;
+  if (E > kSmemEntries) {
+    unsigned H = 64;
+    while (H < 2u * static_cast<unsigned>(E)) H <<= 1;
+    if (tid == 0) {
+      big = ScratchAlloc(P.scratch, P.scratch_cap, P.ctl,
+                         static_cast<unsigned long long>(E) * 16ull + static_cast<unsigned long long>(H) * 4ull, P.err);
+    }
+    __syncthreads();
+    if (big == nullptr) {
+      if (tid == 0) P.cand_cnt[gid] = 0;
+      return;
+    }
+    unsigned char* b = reinterpret_cast<unsigned char*>(big);
+    heads = reinterpret_cast<int*>(b);
+    et = reinterpret_cast<int*>(b + 4ull * H);
+    ei = et + E;
+    ee = reinterpret_cast<unsigned*>(ei + E);
+    enx = reinterpret_cast<int*>(ee + E);
+    hmask = H - 1;
+  }
+  for (unsigned h = tid; h <= hmask; h += kPrepThreads) heads[h] = -1;
+  // per-group pair tables
+  const long long gg = static_cast<long long>(g) * g;
+  unsigned char* mat = P.mat + P.mat_off[gid];
+  long long* pmat = reinterpret_cast<long long*>(mat);
+  double* rmat = reinterpret_cast<double*>(mat + 8 * gg);
+  int* cmat = reinterpret_cast<int*>(mat + 16 * gg);
+  unsigned char* fmat = mat + 20 * gg;
+  for (long long k = tid; k < gg; k += kPrepThreads) {
+    pmat[k] = 0;
+    fmat[k] = 0;
+  }
+  __syncthreads();
+  // entries, approximate old costs and direct in-group edges
+  for (int i = warp; i < g; i += nwarps) {
+    const int rep = S.q[i];
+    const long long si = S.sz[i];
+    const Entry* row = Q.ent + S.off[i];
+    const int len = S.len[i];
+    const int eo = S.eoff[i];
+    long long old = 0;
+    for (int k = lane; k < len; k += 32) {
+      const Entry e = row[k];
+      const int t = EntNb(e);
+      const long long c = EntCnt(e);
+      const long long st = Q.size[t];
+      old += EncodeCostForPair(rep, si, t, st, c);
+      et[eo + k] = t;
+      ei[eo + k] = i;
+      ee[eo + k] = static_cast<unsigned>(c);
+      enx[eo + k] = atomicExch(&heads[BucketHash(t, hmask)], eo + k);
+      if (P.group_of[t] == gid) {
+        const int j = P.idx_in_group[t];
+        if (i < j) atomicAdd(reinterpret_cast<unsigned long long*>(&pmat[static_cast<long long>(i) * g + j]),
+                             static_cast<unsigned long long>(c));
+      }
+    }
+    old = WarpSum(old);
+    if (lane == 0) {
+      const long long internal = Q.internal[rep];
+      if (internal > 0) old += EncodeCostForPair(rep, si, rep, si, 2 * internal);
+      S.old[i] = old;
+    }
+  }
+  __syncthreads();
+  // every two members sharing a target: proxy += max(0, old - new)
+  unsigned long long examined = 0;
+  for (int idx = tid; idx < E; idx += kPrepThreads) {
+    const int t = et[idx];
+    const int i = ei[idx];
+    const long long c = ee[idx];
+    long long st = -1;
+    for (int k = enx[idx]; k != -1; k = enx[k]) {
+      if (et[k] != t) continue;
+      if (st < 0) st = Q.size[t];
+      const int j = ei[k];
+      const int a = i < j ? i : j;
+      const int b = i < j ? j : i;
+      const long long ea = a == i ? c : static_cast<long long>(ee[k]);
+      const long long eb = a == i ? static_cast<long long>(ee[k]) : c;
+      const long long sa = S.sz[a];
+      const long long sb = S.sz[b];
+      const int qa = S.q[a];
+      const int qb = S.q[b];
+      ++examined;
+      const long long oldc = EncodeCostForPair(qa, sa, t, st, ea) + EncodeCostForPair(qb, sb, t, st, eb);
+      const long long newc = EncodeCostForPair(qa, sa + sb, t, st, ea + eb);
+      const long long delta = oldc - newc;
+      if (delta > 0) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&pmat[static_cast<long long>(a) * g + b]),
+                  static_cast<unsigned long long>(delta));
+      }
+    }
+  }
+  examined = WarpSum(static_cast<long long>(examined));
+  if (lane == 0 && examined) atomicAdd(&S.examined, examined);
+  __syncthreads();
+  // per member: candidates with positive proxy, ratio, top-k
+  int top_k = P.top_k < g - 1 ? P.top_k : g - 1;
+  if (top_k < 1) top_k = 1;
+  for (int i = warp; i < g; i += nwarps) {
+    int cnt = 0;
+    double* rrow = rmat + static_cast<long long>(i) * g;
+    int* crow = cmat + static_cast<long long>(i) * g;
+    for (int base = 0; base < g; base += 32) {
+      const int j = base + lane;
+      long long pg = 0;
+      if (j < g && j != i) {
+        const int a = i < j ? i : j;
+        const int b = i < j ? j : i;
+        pg = pmat[static_cast<long long>(a) * g + b];
+      }
+      const bool pred = pg > 0;
+      const unsigned ball = __ballot_sync(0xffffffffu, pred);
+      if (pred) {
+        const int pos = cnt + __popc(ball & ((1u << lane) - 1u));
+        const int a = i < j ? i : j;
+        const int b = i < j ? j : i;
+        long long denom = S.old[a] + S.old[b];
+        if (denom < 1) denom = 1;
+        rrow[pos] = static_cast<double>(pg) / static_cast<double>(denom);
+        crow[pos] = j;
+      }
+      cnt += __popc(ball);
+    }
+    __syncwarp();
+    const int qi = S.q[i];
+    if (cnt <= top_k) {
+      for (int c = lane; c < cnt; c += 32) {
+        const int j = crow[c];
+        const int a = i < j ? i : j;
+        const int b = i < j ? j : i;
+        fmat[static_cast<long long>(a) * g + b] = 1;
+      }
+    } else {
+      RankKey prev;
+      bool have_prev = false;
+      for (int r = 0; r < top_k; ++r) {
+        RankKey best;
+        bool have = false;
+        for (int c = lane; c < cnt; c += 32) {
+          RankKey k;
+          k.j = crow[c];
+          const int a = i < k.j ? i : k.j;
+          const int b = i < k.j ? k.j : i;
+          k.ratio = rrow[c];
+          k.pg = pmat[static_cast<long long>(a) * g + b];
+          const int qj = S.q[k.j];
+          k.lo = qi < qj ? qi : qj;
+          k.hi = qi < qj ? qj : qi;
+          if (have_prev && !Better(prev, k)) continue;
+          if (!have || Better(k, best)) {
+            best = k;
+            have = true;
+          }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          RankKey other;
+          other.ratio = __shfl_xor_sync(0xffffffffu, best.ratio, o);
+          other.pg = __shfl_xor_sync(0xffffffffu, best.pg, o);
+          other.lo = __shfl_xor_sync(0xffffffffu, best.lo, o);
+          other.hi = __shfl_xor_sync(0xffffffffu, best.hi, o);
+          other.j = __shfl_xor_sync(0xffffffffu, best.j, o);
+          const int ohave = __shfl_xor_sync(0xffffffffu, have ? 1 : 0, o);
+          if (ohave && (!have || Better(other, best))) {
+            best = other;
+            have = true;
+          }
+        }
+        if (!have) break;
+        if (lane == 0) {
+          const int a = i < best.j ? i : best.j;
+          const int b = i < best.j ? best.j : i;
+          fmat[static_cast<long long>(a) * g + b] = 1;
+        }
+        prev = best;
+        have_prev = true;
+      }
+    }
+  }
+  __syncthreads();
+  // union of kept pairs in (a_idx, b_idx) order
+  for (int a = warp; a < g; a += nwarps) {
+    int cnt = 0;
+    for (int base = a + 1; base < g; base += 32) {
+      const int b = base + lane;
+      const bool f = b < g && fmat[static_cast<long long>(a) * g + b];
+      cnt += __popc(__ballot_sync(0xffffffffu, f));
+    }
+    if (lane == 0) S.eoff[a] = cnt;
+  }
+  __syncthreads();
+  if (tid == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < g; base += kPrepThreads) {
+    const int i = base + tid;
+    const int v = i < g ? S.eoff[i] : 0;
+    int ex = 0, agg = 0;
+    BlockScan(scan_tmp).ExclusiveSum(v, ex, agg);
+    __syncthreads();
+    if (i < g) S.eoff[i] = carry + ex;
+    __syncthreads();
+    if (tid == 0) carry += agg;
+    __syncthreads();
+  }
+  const int nc = carry;
+  int2* out = P.cand + P.cand_off[gid];
+  for (int a = warp; a < g; a += nwarps) {
+    int pos = S.eoff[a];
+    for (int base = a + 1; base < g; base += 32) {
+      const int b = base + lane;
+      const bool f = b < g && fmat[static_cast<long long>(a) * g + b];
+      const unsigned ball = __ballot_sync(0xffffffffu, f);
+      if (f) out[pos + __popc(ball & ((1u << lane) - 1u))] = make_int2(a, b);
+      pos += __popc(ball);
+    }
+  }
+  if (tid == 0) {
+    P.cand_cnt[gid] = nc;
+    atomicAdd(&P.stats[kStGroupCount], 1ull);
+    atomicMax(&P.stats[kStGroupMaxSize], static_cast<unsigned long long>(g));
+    atomicAdd(&P.stats[kStRawPairCount], static_cast<unsigned long long>(g) * (g - 1) / 2);
+    atomicAdd(&P.stats[kStCandAfterPrune], static_cast<unsigned long long>(nc));
+    atomicAdd(&P.stats[kStProxyExamined], S.examined);
+    // algorithmic bytes: member rows (8 B/entry) + target size gathers (4 B/entry)
+    atomicAdd(&P.stats[kStPrepareBytes], 12ull * static_cast<unsigned long long>(E));
+  }
+}
+
+// ------------------------------------------------------------ score
+
+struct ScoreParams {
+  QuotientView Q;
+  const int* order;
+  const int* gstart;
+  int g0;
+  const long long* cand_off;
+  const int2* cand;
+  const int* cand_cnt;
+  longlong2* res;
+  unsigned long long* stats;
+  DevError* err;
+};
+
+__device__ __forceinline__ void FlushScoreStats(unsigned long long* stats, const GainWork& w, long long pairs,
+                                                long long view_nnz) {
+  if (pairs == 0) return;
+  atomicAdd(&stats[kStExactCalls], static_cast<unsigned long long>(pairs));
+  atomicAdd(&stats[kStInputNnz], static_cast<unsigned long long>(view_nnz));
+  atomicAdd(&stats[kStRawA], static_cast<unsigned long long>(w.raw_a));
+  atomicAdd(&stats[kStRawB], static_cast<unsigned long long>(w.raw_b));
+  atomicAdd(&stats[kStUnion], static_cast<unsigned long long>(w.uni));
+  atomicAdd(&stats[kStOverlap], static_cast<unsigned long long>(w.ovl));
+  // algorithmic bytes: 8 B per row entry read, 4 B per union-neighbour size
+  // gather, 8 B pair + 16 B result per pair
+  atomicAdd(&stats[kStScoreBytes],
+            static_cast<unsigned long long>(8 * (w.raw_a + w.raw_b) + 4 * w.uni + 24 * pairs));
+}
+
+__global__ void __launch_bounds__(kScoreThreads) ScoreKernel(ScoreParams P) {
+  const int gid = P.g0 + blockIdx.x;
+  const int cnt = P.cand_cnt[gid];
+  const int p0 = blockIdx.y * kPairsPerScoreCta;
+  if (p0 >= cnt) return;
+  const int p1 = min(cnt, p0 + kPairsPerScoreCta);
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long base = P.cand_off[gid];
+  const int* q = P.order + P.gstart[gid];
+  GainWork w = {0, 0, 0, 0};
+  long long pairs = 0, view_nnz = 0;
+  for (int p = p0 + warp; p < p1; p += kScoreThreads / 32) {
+    const int2 c = P.cand[base + p];
+    const int a = q[c.x];
+    const int b = q[c.y];
+    long long gain = 0, before = 0;
+    WarpExactGain(P.Q, a, b, &gain, &before, &w, P.err);
+    if (lane == 0) {
+      P.res[base + p] = make_longlong2(gain, before);
+      ++pairs;
+      view_nnz += P.Q.len[a] + (P.Q.internal[a] > 0 ? 1 : 0) + P.Q.len[b] + (P.Q.internal[b] > 0 ? 1 : 0);
+    }
+  }
+  if (lane == 0) FlushScoreStats(P.stats, w, pairs, view_nnz);
+}
+
+// Scoring service over an explicit pair list (ScoreCandidatesCuda's role).
+__global__ void __launch_bounds__(kScoreThreads) ScorePairsKernel(QuotientView Q, const int* rep_a,
+                                                                  const int* rep_b, long long count,
+                                                                  longlong2* res, DevError* err) {
+  const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  for (long long p = warp; p < count; p += nw) {
+    const int a = rep_a[p];
+    const int b = rep_b[p];
+    if (a == b || Q.size[a] <= 0 || Q.size[b] <= 0) {
+      if (lane == 0) {
+        RaiseError(err, kErrInactive, a, b, 0);
+        res[p] = make_longlong2(0, 0);
+      }
+      continue;
+    }
+    long long gain = 0, before = 0;
+    WarpExactGain(Q, a, b, &gain, &before, nullptr, err);
+    if (lane == 0) res[p] = make_longlong2(gain, before);
+  }
+}
+
+// ------------------------------------------------------------ select
+
+struct SelectParams {
+  const int* order;
+  const int* gstart;
+  const int* glen;
+  int g0;
+  const long long* cand_off;
+  const int2* cand;
+  const int* cand_cnt;
+  const longlong2* res;
+  const long long* sel_off;
+  int* sel_keep;
+  int* sel_rem;
+  long long* sel_gain;
+  int* sel_cnt;
+  double threshold;
+  int use_threshold;
+  unsigned char* scratch;
+  unsigned long long scratch_cap;
+  BlockCtl* ctl;
+  unsigned long long* stats;
+  DevError* err;
+};
+
+// In-place ascending bitonic sort of n (power of two) keys by one CTA.
+__device__ void CtaBitonicSort(unsigned long long* keys, int n) {
+  for (int k = 2; k <= n; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const unsigned long long a = keys[i];
+          const unsigned long long b = keys[ixj];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) {
+            keys[i] = b;
+            keys[ixj] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kSelectThreads) SelectKernel(SelectParams P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned long long* skeys = reinterpret_cast<unsigned long long*>(smem_raw);
+  __shared__ unsigned char used[kMaxGroup];
+  __shared__ int nkeys;
+  __shared__ unsigned long long* gkeys;
+  __shared__ unsigned long long rej_thr, positive;
+  const int tid = threadIdx.x;
+  const int gid = P.g0 + blockIdx.x;
+  const int g = P.glen[gid];
+  const int cnt = g >= 2 && g <= kMaxGroup ? P.cand_cnt[gid] : 0;
+  if (cnt == 0) {
+    if (tid == 0) P.sel_cnt[gid] = 0;
+    return;
+  }
+  int cap = 1;
+  while (cap < cnt) cap <<= 1;
+  if (tid == 0) {
+    nkeys = 0;
+    rej_thr = 0;
+    positive = 0;
+    gkeys = cap <= kSelectSmemKeys ? skeys
+                                   : ScratchAlloc(P.scratch, P.scratch_cap, P.ctl, 8ull * cap, P.err);
+  }
+  for (int i = tid; i < g; i += kSelectThreads) used[i] = 0;
+  __syncthreads();
+  unsigned long long* keys = gkeys;
+  if (keys == nullptr) {
+    if (tid == 0) P.sel_cnt[gid] = 0;
+    return;
+  }
+  const long long base = P.cand_off[gid];
+  unsigned long long my_rej = 0, my_pos = 0;
+  for (int c = tid; c < cnt; c += kSelectThreads) {
+    const longlong2 r = P.res[base + c];
+    const long long gain = r.x;
+    const long long before = r.y;
+    if (gain <= 0) {
+      ++my_rej;
+      continue;
+    }
+    if (P.use_threshold) {
+      if (before <= 0) {
+        ++my_rej;
+        continue;
+      }
+      const double ratio = static_cast<double>(gain) / static_cast<double>(before);
+      if (ratio < P.threshold) {
+        ++my_rej;
+        continue;
+      }
+    }
+    ++my_pos;
+    if (gain > kKeyGainMax) RaiseError(P.err, kErrKeyRange, gid, c, 0);
+    const int2 ab = P.cand[base + c];
+    const unsigned long long key = (static_cast<unsigned long long>(kKeyGainMax - gain) << (2 * kKeyIdxBits)) |
+                                   (static_cast<unsigned long long>(ab.x) << kKeyIdxBits) |
+                                   static_cast<unsigned long long>(ab.y);
+    keys[atomicAdd(&nkeys, 1)] = key;
+  }
+  if (my_rej) atomicAdd(&rej_thr, my_rej);
+  if (my_pos) atomicAdd(&positive, my_pos);
+  __syncthreads();
+  const int m = nkeys;
+  int pow2 = 1;
+  while (pow2 < m) pow2 <<= 1;
+  for (int i = m + tid; i < pow2; i += kSelectThreads) keys[i] = ~0ull;
+  __syncthreads();
+  if (m > 1) CtaBitonicSort(keys, pow2);
+  if (tid == 0) {
+    const int* q = P.order + P.gstart[gid];
+    const long long so = P.sel_off[gid];
+    int ns = 0;
+    long long total = 0;
+    unsigned long long overlap = 0;
+    const unsigned long long idx_mask = (1ull << kKeyIdxBits) - 1;
+    for (int k = 0; k < m; ++k) {
+      const unsigned long long key = keys[k];
+      const int b = static_cast<int>(key & idx_mask);
+      const int a = static_cast<int>((key >> kKeyIdxBits) & idx_mask);
+      const long long gain = kKeyGainMax - static_cast<long long>(key >> (2 * kKeyIdxBits));
+      if (used[a] || used[b]) {
+        ++overlap;
+        continue;
+      }
+      used[a] = 1;
+      used[b] = 1;
+      P.sel_keep[so + ns] = q[a];
+      P.sel_rem[so + ns] = q[b];
+      P.sel_gain[so + ns] = gain;
+      ++ns;
+      total += gain;
+    }
+    P.sel_cnt[gid] = ns;
+    atomicAdd(&P.stats[kStRejThreshold], rej_thr);
+    atomicAdd(&P.stats[kStPositive], positive);
+    atomicAdd(&P.stats[kStRejOverlap], overlap);
+    atomicAdd(&P.stats[kStCandPairs], static_cast<unsigned long long>(m));
+    atomicAdd(&P.stats[kStSelected], static_cast<unsigned long long>(ns));
+    atomicAdd(&P.stats[kStLocalGain], static_cast<unsigned long long>(total));
+  }
+}
+
+// ------------------------------------------------------------ commit
+
+struct CommitParams {
+  QuotientView Q;
+  int g0;
+  const long long* sel_off;
+  const int* sel_keep;
+  const int* sel_rem;
+  const long long* sel_gain;
+  const int* sel_cnt;
+  unsigned char* sel_ok;
+  int check_gain;
+  // Update_S state
+  int* head;
+  int* next;
+  int* tail;
+  int* fwd;
+  int* stamp;
+  int* partner;
+  int* claim;
+  int block_stamp;
+  int* acc_keep;
+  int* acc_rem;
+  int* aff;
+  BlockCtl* ctl;
+  unsigned long long* stats;
+  DevError* err;
+};
+
+// Commit-time validation: ExactMergeGainPersistent of each selected pair
+// against the block-start state; accepted iff gain > 0. The scored gain was
+// computed on the same state, so a difference is an internal error.
+__global__ void __launch_bounds__(256) ValidateKernel(CommitParams P) {
+  const int gid = P.g0 + blockIdx.x;
+  const int cnt = P.sel_cnt[gid];
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long so = P.sel_off[gid];
+  for (int s = warp; s < cnt; s += 8) {
+    const int k = P.sel_keep[so + s];
+    const int r = P.sel_rem[so + s];
+    long long gain = 0, before = 0;
+    GainWork w = {0, 0, 0, 0};
+    WarpExactGain(P.Q, k, r, &gain, &before, &w, P.err);
+    if (lane == 0) {
+      if (P.check_gain && gain != P.sel_gain[so + s]) RaiseError(P.err, kErrValidation, k, r, 0);
+      P.sel_ok[so + s] = gain > 0 ? 1 : 0;
+      atomicAdd(&P.stats[kStValidationCalls], 1ull);
+      atomicAdd(&P.stats[kStValidationWork], static_cast<unsigned long long>(w.raw_a + w.raw_b));
+      atomicAdd(&P.stats[kStIsolatedGain], static_cast<unsigned long long>(P.sel_gain[so + s]));
+      if (gain <= 0) atomicAdd(&P.stats[kStRejNonpositive], 1ull);
+    }
+  }
+}
+
+// Update_S for the accepted pairs: sizes, internal counts, member lists,
+// forwarding; records the block's merges and claims every neighbour row of a
+// removed supernode for the row pass.
+__global__ void __launch_bounds__(256) ApplyKernel(CommitParams P) {
+  const int gid = P.g0 + blockIdx.x;
+  const int cnt = P.sel_cnt[gid];
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long so = P.sel_off[gid];
+  const QuotientView& Q = P.Q;
+  for (int s = warp; s < cnt; s += 8) {
+    if (!P.sel_ok[so + s]) continue;
+    const int k = P.sel_keep[so + s];
+    const int r = P.sel_rem[so + s];
+    const Entry* rr = Q.ent + Q.off[r];
+    const int lr = Q.len[r];
+    if (lane == 0) {
+      const long long ekr = RowLookup(Q.ent + Q.off[k], Q.len[k], r);
+      Q.internal[k] += Q.internal[r] + ekr;
+      Q.internal[r] = 0;
+      Q.size[k] += Q.size[r];
+      Q.size[r] = 0;
+      P.next[P.tail[k]] = P.head[r];
+      P.tail[k] = P.tail[r];
+      P.head[r] = -1;
+      P.fwd[r] = k;
+      P.stamp[k] = 2 * P.block_stamp;
+      P.stamp[r] = 2 * P.block_stamp + 1;
+      P.partner[k] = r;
+      P.partner[r] = k;
+      const unsigned idx = atomicAdd(&P.ctl->acc_cnt, 1u);
+      P.acc_keep[idx] = k;
+      P.acc_rem[idx] = r;
+      atomicAdd(&P.stats[kStAccepted], 1ull);
+      atomicAdd(&P.stats[kStTouched], static_cast<unsigned long long>(2 + 3 * (lr - (ekr > 0 ? 1 : 0))));
+    }
+    for (int i = lane; i < lr; i += 32) {
+      const int x = EntNb(rr[i]);
+      if (x == k) continue;
+      if (atomicExch(&P.claim[x], P.block_stamp) != P.block_stamp) {
+        P.aff[atomicAdd(&P.ctl->aff_cnt, 1u)] = x;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------ rows
+
+struct RowsParams {
+  QuotientView Q;
+  const int* stamp;
+  const int* partner;
+  int block_stamp;
+  const int* acc_keep;
+  const int* acc_rem;
+  const int* aff;
+  BlockCtl* ctl;
+  unsigned long long* pool_top;
+  unsigned long long pool_cap;
+  unsigned char* scratch;
+  unsigned long long scratch_cap;
+  unsigned long long* stats;
+  DevError* err;
+};
+
+struct RowsSmem {
+  Entry s[kRowSmem];
+  int d[kRowSmem + 1];
+  Entry ins[kRowSmem];
+};
+
+// Rewrites a staged sorted row S[0..L) (adjacent equal ids allowed: the keep
+// row is staged as the merge of two rows) into out: duplicates are summed,
+// ids sk / sr are dropped, entries of supernodes removed in this block move
+// to their keep partner (summed into its entry, or inserted at its sorted
+// position). Returns the new length.
+__device__ int RewriteRow(const RowsParams& P, Entry* S, int L, int* D, Entry* INS, int sk, int sr, Entry* out) {
+  using BlockScan = cub::BlockScan<int, kRowsThreads>;
+  __shared__ typename BlockScan::TempStorage scan_tmp;
+  __shared__ int nins, carry;
+  const int tid = threadIdx.x;
+  const int remove_stamp = 2 * P.block_stamp + 1;
+  if (tid == 0) {
+    nins = 0;
+    carry = 0;
+  }
+  for (int i = tid; i < L; i += kRowsThreads) {
+    int drop = 0;
+    if (i > 0 && EntNb(S[i]) == EntNb(S[i - 1])) {
+      atomicAdd(reinterpret_cast<unsigned long long*>(&S[i - 1]), static_cast<unsigned long long>(EntCnt(S[i])));
+      drop = 1;
+    }
+    D[i] = drop;
+  }
+  __syncthreads();
+  for (int i = tid; i < L; i += kRowsThreads) {
+    if (D[i]) continue;
+    const int id = EntNb(S[i]);
+    if (id == sk || id == sr) {
+      D[i] = 1;
+      continue;
+    }
+    if (P.stamp[id] == remove_stamp) {
+      const int kp = P.partner[id];
+      D[i] = 1;
+      if (kp == sk) continue;
+      const int p = RowLowerBound(S, L, kp);
+      const long long c = EntCnt(S[i]);
+      if (p < L && EntNb(S[p]) == kp) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&S[p]), static_cast<unsigned long long>(c));
+      } else {
+        INS[atomicAdd(&nins, 1)] = MakeEnt(kp, c);
+      }
+    }
+  }
+  __syncthreads();
+  // exclusive scan of drop flags (D[L] = total)
+  for (int base = 0; base < L; base += kRowsThreads) {
+    const int i = base + tid;
+    const int v = i < L ? D[i] : 0;
+    int ex = 0, agg = 0;
+    BlockScan(scan_tmp).ExclusiveSum(v, ex, agg);
+    __syncthreads();
+    if (i < L) D[i] = carry + ex;
+    __syncthreads();
+    if (tid == 0) carry += agg;
+    __syncthreads();
+  }
+  if (tid == 0) D[L] = carry;
+  const int m = nins;
+  int pow2 = 1;
+  while (pow2 < m) pow2 <<= 1;
+  for (int i = m + tid; i < pow2; i += kRowsThreads) INS[i] = ~0ull;
+  __syncthreads();
+  if (m > 1) CtaBitonicSort(INS, pow2);
+  for (int i = tid; i < L; i += kRowsThreads) {
+    if (D[i + 1] != D[i]) continue;  // dropped
+    const Entry e = S[i];
+    const int pos = i - D[i] + RowLowerBound(INS, m, EntNb(e));
+    out[pos] = e;
+  }
+  for (int j = tid; j < m; j += kRowsThreads) {
+    const Entry e = INS[j];
+    const int p = RowLowerBound(S, L, EntNb(e));
+    out[j + p - D[p]] = e;
+  }
+  __syncthreads();
+  return L - D[L] + m;
+}
+
+__global__ void __launch_bounds__(kRowsThreads) RowsKernel(RowsParams P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  RowsSmem& R = *reinterpret_cast<RowsSmem*>(smem_raw);
+  __shared__ Entry* gbuf;
+  __shared__ long long new_off;
+  const QuotientView& Q = P.Q;
+  const int acc = static_cast<int>(P.ctl->acc_cnt);
+  const int total = acc + static_cast<int>(P.ctl->aff_cnt);
+  const int tid = threadIdx.x;
+  for (int w = blockIdx.x; w < total; w += gridDim.x) {
+    int sk = -1, sr = -1, row = -1;
+    if (w < acc) {
+      sk = P.acc_keep[w];
+      sr = P.acc_rem[w];
+    } else {
+      row = P.aff[w - acc];
+      if ((P.stamp[row] >> 1) == P.block_stamp) continue;  // keep/remove rows are rebuilt separately
+    }
+    const int L = w < acc ? Q.len[sk] + Q.len[sr] : Q.len[row];
+    Entry* S = R.s;
+    int* D = R.d;
+    Entry* INS = R.ins;
+    if (L > kRowSmem) {
+      int pow2 = 1;
+      while (pow2 < L) pow2 <<= 1;
+      if (tid == 0) {
+        gbuf = reinterpret_cast<Entry*>(ScratchAlloc(P.scratch, P.scratch_cap, P.ctl,
+                                                     8ull * L + 4ull * (L + 1) + 8ull * pow2 + 512ull, P.err));
+      }
+      __syncthreads();
+      if (gbuf == nullptr) return;
+      S = gbuf;
+      INS = S + L;
+      D = reinterpret_cast<int*>(INS + pow2);
+    }
+    if (w < acc) {
+      // stage merge(row k, row r): A entries before B entries on equal ids
+      const Entry* A = Q.ent + Q.off[sk];
+      const Entry* B = Q.ent + Q.off[sr];
+      const int la = Q.len[sk];
+      const int lb = Q.len[sr];
+      for (int i = tid; i < la; i += kRowsThreads) {
+        const Entry e = A[i];
+        S[i + RowLowerBound(B, lb, EntNb(e))] = e;
+      }
+      for (int j = tid; j < lb; j += kRowsThreads) {
+        const Entry e = B[j];
+        const int key = EntNb(e);
+        int lo = 0, hi = la;  // upper bound in A
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (EntNb(A[mid]) <= key) lo = mid + 1; else hi = mid;
+        }
+        S[j + lo] = e;
+      }
+      if (tid == 0) {
+        const unsigned long long want = static_cast<unsigned long long>(L > 0 ? L : 1);
+        const unsigned long long at = atomicAdd(P.pool_top, want);
+        if (at + want > P.pool_cap) {
+          RaiseError(P.err, kErrPool, sk, L, 0);
+          new_off = -1;
+        } else {
+          new_off = static_cast<long long>(at);
+        }
+      }
+      __syncthreads();
+      if (new_off < 0) return;
+      const int nl = RewriteRow(P, S, L, D, INS, sk, sr, Q.ent + new_off);
+      if (tid == 0) {
+        Q.off[sk] = new_off;
+        Q.len[sk] = nl;
+        Q.cap[sk] = L > 0 ? L : 1;
+        Q.len[sr] = 0;
+        atomicAdd(&P.stats[kStUpdateBytes], 8ull * (2ull * L + nl));
+      }
+    } else {
+      Entry* rowp = Q.ent + Q.off[row];
+      for (int i = tid; i < L; i += kRowsThreads) S[i] = rowp[i];
+      __syncthreads();
+      const int nl = RewriteRow(P, S, L, D, INS, -1, -1, rowp);
+      if (tid == 0) {
+        Q.len[row] = nl;
+        atomicAdd(&P.stats[kStRowsRewritten], 1ull);
+        atomicAdd(&P.stats[kStRowEntriesRewritten], static_cast<unsigned long long>(L));
+        atomicAdd(&P.stats[kStUpdateBytes], 8ull * (L + nl));
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void ScatterGroupKernel(const int* __restrict__ q, const int* __restrict__ idx, int g,
+                                   int* __restrict__ group_of, int* __restrict__ idx_in_group) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < g) {
+    group_of[q[i]] = 0;
+    idx_in_group[q[i]] = idx[i];
+  }
+}
+
+__global__ void RelabelKernel(int* __restrict__ label, const int* __restrict__ fwd, int n) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < n) label[v] = fwd[label[v]];
+}
+
+}  // namespace
+
+// --------------------------------------------------------------- host side
+
+void Engine::ConfigureKernels() {
+  CheckCuda(cudaFuncSetAttribute(PrepareKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(sizeof(PrepSmem))), "prepare smem attribute");
+  CheckCuda(cudaFuncSetAttribute(SelectKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 8 * kSelectSmemKeys), "select smem attribute");
+  CheckCuda(cudaFuncSetAttribute(RowsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(sizeof(RowsSmem))), "rows smem attribute");
+}
+
+void Engine::PrepareIterationBuffers() {
+  const int64_t G = n_groups_;
+  h_cand_off_.assign(static_cast<size_t>(G) + 1, 0);
+  h_sel_off_.assign(static_cast<size_t>(G) + 1, 0);
+  h_mat_off_.assign(static_cast<size_t>(G) + 1, 0);
+  long long max_mat = 0;
+  const long long k = cfg_.top_k > 0 ? cfg_.top_k : 1;
+  for (int64_t gi = 0; gi < G; ++gi) {
+    const long long g = h_glen_[static_cast<size_t>(gi)];
+    const long long pairs = g >= 2 ? std::min(g * (g - 1) / 2, g * k) : 0;
+    h_cand_off_[static_cast<size_t>(gi) + 1] = h_cand_off_[static_cast<size_t>(gi)] + pairs;
+    h_sel_off_[static_cast<size_t>(gi) + 1] = h_sel_off_[static_cast<size_t>(gi)] + (g >= 2 ? g / 2 : 0);
+  }
+  const int64_t bs = cfg_.group_batch_size;
+  for (int64_t b0 = 0; b0 < G; b0 += bs) {
+    const int64_t b1 = std::min(G, b0 + bs);
+    long long off = 0;
+    for (int64_t gi = b0; gi < b1; ++gi) {
+      const long long g = h_glen_[static_cast<size_t>(gi)];
+      h_mat_off_[static_cast<size_t>(gi)] = off;
+      if (g >= 2) off += (21 * g * g + 255) & ~255ll;
+    }
+    max_mat = std::max(max_mat, off);
+  }
+  d_cand_off_.ensure(static_cast<size_t>(G) + 1);
+  d_sel_off_.ensure(static_cast<size_t>(G) + 1);
+  d_mat_off_.ensure(static_cast<size_t>(G) + 1);
+  d_cand_cnt_.ensure(static_cast<size_t>(G) + 1);
+  d_sel_cnt_.ensure(static_cast<size_t>(G) + 1);
+  const size_t ncand = static_cast<size_t>(h_cand_off_[static_cast<size_t>(G)]);
+  d_cand_.ensure(ncand + 1);
+  d_res_.ensure(ncand + 1);
+  const size_t nsel = static_cast<size_t>(h_sel_off_[static_cast<size_t>(G)]);
+  d_sel_keep_.ensure(nsel + 1);
+  d_sel_rem_.ensure(nsel + 1);
+  d_sel_gain_.ensure(nsel + 1);
+  d_sel_ok_.ensure(nsel + 1);
+  d_mat_.ensure(static_cast<size_t>(max_mat) + 256);
+  if (G > 0) {
+    CheckCuda(cudaMemcpyAsync(d_cand_off_.p, h_cand_off_.data(), sizeof(long long) * static_cast<size_t>(G + 1),
+                              cudaMemcpyHostToDevice, stream_), "h2d cand_off");
+    CheckCuda(cudaMemcpyAsync(d_sel_off_.p, h_sel_off_.data(), sizeof(long long) * static_cast<size_t>(G + 1),
+                              cudaMemcpyHostToDevice, stream_), "h2d sel_off");
+    CheckCuda(cudaMemcpyAsync(d_mat_off_.p, h_mat_off_.data(), sizeof(long long) * static_cast<size_t>(G + 1),
+                              cudaMemcpyHostToDevice, stream_), "h2d mat_off");
+  }
+}
+
+QuotientView Engine::View() {
+  QuotientView Q;
+  Q.ent = d_pool_[cur_pool_].p;
+  Q.off = d_qoff_.p;
+  Q.len = d_qlen_.p;
+  Q.cap = d_qcap_.p;
+  Q.size = d_qsize_.p;
+  Q.internal = d_qint_.p;
+  return Q;
+}
+
+void Engine::LaunchCommit(int64_t g0, int nbg, bool check_gain) {
+  CommitParams C;
+  C.Q = View();
+  C.g0 = static_cast<int>(g0);
+  C.sel_off = d_sel_off_.p;
+  C.sel_keep = d_sel_keep_.p;
+  C.sel_rem = d_sel_rem_.p;
+  C.sel_gain = d_sel_gain_.p;
+  C.sel_cnt = d_sel_cnt_.p;
+  C.sel_ok = d_sel_ok_.p;
+  C.check_gain = check_gain ? 1 : 0;
+  C.head = d_head_.p;
+  C.next = d_next_.p;
+  C.tail = d_tail_.p;
+  C.fwd = d_fwd_.p;
+  C.stamp = d_stamp_.p;
+  C.partner = d_partner_.p;
+  C.claim = d_claim_.p;
+  C.block_stamp = block_stamp_;
+  C.acc_keep = d_acc_keep_.p;
+  C.acc_rem = d_acc_rem_.p;
+  C.aff = d_aff_.p;
+  C.ctl = d_ctl_.p;
+  C.stats = d_stats_.p;
+  C.err = d_err_.p;
+  if (check_gain) ValidateKernel<<<nbg, 256, 0, stream_>>>(C);
+  ApplyKernel<<<nbg, 256, 0, stream_>>>(C);
+  RowsParams R;
+  R.Q = View();
+  R.stamp = d_stamp_.p;
+  R.partner = d_partner_.p;
+  R.block_stamp = block_stamp_;
+  R.acc_keep = d_acc_keep_.p;
+  R.acc_rem = d_acc_rem_.p;
+  R.aff = d_aff_.p;
+  R.ctl = d_ctl_.p;
+  R.pool_top = d_pool_top_.p;
+  R.pool_cap = pool_cap_;
+  R.scratch = d_scratch_.p;
+  R.scratch_cap = d_scratch_.n;
+  R.stats = d_stats_.p;
+  R.err = d_err_.p;
+  BeginTimed(kTimeUpdate);
+  RowsKernel<<<kRowsGrid, kRowsThreads, sizeof(RowsSmem), stream_>>>(R);
+  EndTimed(kTimeUpdate);
+}
+
+void Engine::RunBlock(int64_t g0, int64_t g1, int64_t max_cap, double threshold) {
+  ++block_stamp_;
+  ++hstats_.blocks;
+  const int nbg = static_cast<int>(g1 - g0);
+  CheckCuda(cudaMemsetAsync(d_ctl_.p, 0, sizeof(BlockCtl), stream_), "memset ctl");
+  PrepareParams PP;
+  PP.Q = View();
+  PP.order = d_order_.p;
+  PP.gstart = d_gstart_.p;
+  PP.glen = d_glen_.p;
+  PP.group_of = d_group_of_.p;
+  PP.idx_in_group = d_idx_in_group_.p;
+  PP.g0 = static_cast<int>(g0);
+  PP.cand_off = d_cand_off_.p;
+  PP.cand = d_cand_.p;
+  PP.cand_cnt = d_cand_cnt_.p;
+  PP.mat_off = d_mat_off_.p;
+  PP.mat = d_mat_.p;
+  PP.scratch = d_scratch_.p;
+  PP.scratch_cap = d_scratch_.n;
+  PP.ctl = d_ctl_.p;
+  PP.top_k = cfg_.top_k;
+  PP.stats = d_stats_.p;
+  PP.err = d_err_.p;
+  BeginTimed(kTimePrepare);
+  PrepareKernel<<<nbg, kPrepThreads, sizeof(PrepSmem), stream_>>>(PP);
+  EndTimed(kTimePrepare);
+  if (max_cap <= 0) return;
+  ScoreParams SP;
+  SP.Q = View();
+  SP.order = d_order_.p;
+  SP.gstart = d_gstart_.p;
+  SP.g0 = static_cast<int>(g0);
+  SP.cand_off = d_cand_off_.p;
+  SP.cand = d_cand_.p;
+  SP.cand_cnt = d_cand_cnt_.p;
+  SP.res = d_res_.p;
+  SP.stats = d_stats_.p;
+  SP.err = d_err_.p;
+  const dim3 sgrid(static_cast<unsigned>(nbg), static_cast<unsigned>((max_cap + kPairsPerScoreCta - 1) / kPairsPerScoreCta));
+  BeginTimed(kTimeScore);
+  ScoreKernel<<<sgrid, kScoreThreads, 0, stream_>>>(SP);
+  EndTimed(kTimeScore);
+  SelectParams LP;
+  LP.order = d_order_.p;
+  LP.gstart = d_gstart_.p;
+  LP.glen = d_glen_.p;
+  LP.g0 = static_cast<int>(g0);
+  LP.cand_off = d_cand_off_.p;
+  LP.cand = d_cand_.p;
+  LP.cand_cnt = d_cand_cnt_.p;
+  LP.res = d_res_.p;
+  LP.sel_off = d_sel_off_.p;
+  LP.sel_keep = d_sel_keep_.p;
+  LP.sel_rem = d_sel_rem_.p;
+  LP.sel_gain = d_sel_gain_.p;
+  LP.sel_cnt = d_sel_cnt_.p;
+  LP.threshold = threshold;
+  LP.use_threshold = cfg_.ea_use_threshold ? 1 : 0;
+  LP.scratch = d_scratch_.p;
+  LP.scratch_cap = d_scratch_.n;
+  LP.ctl = d_ctl_.p;
+  LP.stats = d_stats_.p;
+  LP.err = d_err_.p;
+  SelectKernel<<<nbg, kSelectThreads, 8 * kSelectSmemKeys, stream_>>>(LP);
+  LaunchCommit(g0, nbg, true);
+}
+
+void Engine::Merge(int iter, int total_iterations) {
+  (void)total_iterations;
+  if (n_groups_ < 0) throw std::runtime_error("Merge requires a preceding Divide");
+  // ComputeMergeThreshold, reciprocal policy (src/sweg.cpp:400-406)
+  const double threshold = 1.0 / static_cast<double>(iter + 1);
+  EnsurePoolRoom();
+  PrepareIterationBuffers();
+  const int64_t G = n_groups_;
+  const int64_t bs = cfg_.group_batch_size;
+  const long long k = cfg_.top_k > 0 ? cfg_.top_k : 1;
+  for (int64_t b0 = 0; b0 < G; b0 += bs) {
+    const int64_t b1 = std::min(G, b0 + bs);
+    int64_t max_cap = 0;
+    for (int64_t gi = b0; gi < b1; ++gi) {
+      const long long g = h_glen_[static_cast<size_t>(gi)];
+      if (g >= 2) max_cap = std::max<int64_t>(max_cap, std::min(g * (g - 1) / 2, g * k));
+    }
+    RunBlock(b0, b1, max_cap, threshold);
+  }
+  RelabelKernel<<<(n_ + 255) / 256, 256, 0, stream_>>>(d_label_.p, d_fwd_.p, n_);
+  n_groups_ = -1;  // the groups are consumed
+  CheckCuda(cudaStreamSynchronize(stream_), "merge sync");
+  CheckError();
+}
+
+void Engine::ScorePairs(const int32_t* rep_a, const int32_t* rep_b, int64_t count, int64_t* gain,
+                        int64_t* before) {
+  if (count <= 0) return;
+  for (int64_t i = 0; i < count; ++i) {
+    if (rep_a[i] < 0 || rep_a[i] >= n_ || rep_b[i] < 0 || rep_b[i] >= n_) {
+      throw std::out_of_range("quotient supernode is out of range");
+    }
+  }
+  DevBuf<int> da, db;
+  DevBuf<longlong2> dr;
+  da.ensure(static_cast<size_t>(count));
+  db.ensure(static_cast<size_t>(count));
+  dr.ensure(static_cast<size_t>(count));
+  CheckCuda(cudaMemcpyAsync(da.p, rep_a, sizeof(int) * static_cast<size_t>(count), cudaMemcpyHostToDevice, stream_),
+            "h2d pairs");
+  CheckCuda(cudaMemcpyAsync(db.p, rep_b, sizeof(int) * static_cast<size_t>(count), cudaMemcpyHostToDevice, stream_),
+            "h2d pairs");
+  const int blocks = static_cast<int>(std::min<int64_t>((count + 7) / 8, 152 * 16));
+  ScorePairsKernel<<<blocks, 256, 0, stream_>>>(View(), da.p, db.p, count, dr.p, d_err_.p);
+  std::vector<longlong2> h(static_cast<size_t>(count));
+  CheckCuda(cudaMemcpyAsync(h.data(), dr.p, sizeof(longlong2) * static_cast<size_t>(count), cudaMemcpyDeviceToHost,
+                            stream_), "d2h results");
+  CheckCuda(cudaStreamSynchronize(stream_), "score sync");
+  da.release();
+  db.release();
+  dr.release();
+  CheckError();
+  for (int64_t i = 0; i < count; ++i) {
+    gain[i] = h[static_cast<size_t>(i)].x;
+    before[i] = h[static_cast<size_t>(i)].y;
+  }
+}
+
+int64_t Engine::PrepareGroup(const int32_t* q, int g, int32_t* a_idx, int32_t* b_idx, int64_t cap) {
+  if (g < 0 || g > kMaxGroup) throw std::invalid_argument("group size out of range");
+  std::vector<int> hq(q, q + g);
+  for (int i = 0; i < g; ++i) {
+    if (hq[static_cast<size_t>(i)] < 0 || hq[static_cast<size_t>(i)] >= n_) {
+      throw std::out_of_range("quotient supernode is out of range");
+    }
+  }
+  // One explicit group; the Divide output is overwritten.
+  n_groups_ = 1;
+  h_glen_.assign(1, g);
+  const int zero = 0;
+  CheckCuda(cudaMemcpyAsync(d_order_.p, hq.data(), sizeof(int) * static_cast<size_t>(g), cudaMemcpyHostToDevice,
+                            stream_), "h2d group");
+  CheckCuda(cudaMemcpyAsync(d_gstart_.p, &zero, sizeof(int), cudaMemcpyHostToDevice, stream_), "h2d gstart");
+  CheckCuda(cudaMemcpyAsync(d_glen_.p, &g, sizeof(int), cudaMemcpyHostToDevice, stream_), "h2d glen");
+  std::vector<int> idx(static_cast<size_t>(g));
+  for (int i = 0; i < g; ++i) idx[static_cast<size_t>(i)] = i;
+  // group_of / idx_in_group for the members: everything else must not match
+  // group 0, so the array is first filled with -1.
+  CheckCuda(cudaMemsetAsync(d_group_of_.p, 0xff, sizeof(int) * static_cast<size_t>(n_), stream_), "memset");
+  DevBuf<int> dq, di;
+  dq.ensure(static_cast<size_t>(g));
+  di.ensure(static_cast<size_t>(g));
+  CheckCuda(cudaMemcpyAsync(dq.p, hq.data(), sizeof(int) * static_cast<size_t>(g), cudaMemcpyHostToDevice, stream_),
+            "h2d");
+  CheckCuda(cudaMemcpyAsync(di.p, idx.data(), sizeof(int) * static_cast<size_t>(g), cudaMemcpyHostToDevice, stream_),
+            "h2d");
+  ScatterGroupKernel<<<(g + 255) / 256, 256, 0, stream_>>>(dq.p, di.p, g, d_group_of_.p, d_idx_in_group_.p);
+  PrepareIterationBuffers();
+  CheckCuda(cudaMemsetAsync(d_ctl_.p, 0, sizeof(BlockCtl), stream_), "memset ctl");
+  PrepareParams PP;
+  PP.Q = View();
+  PP.order = d_order_.p;
+  PP.gstart = d_gstart_.p;
+  PP.glen = d_glen_.p;
+  PP.group_of = d_group_of_.p;
+  PP.idx_in_group = d_idx_in_group_.p;
+  PP.g0 = 0;
+  PP.cand_off = d_cand_off_.p;
+  PP.cand = d_cand_.p;
+  PP.cand_cnt = d_cand_cnt_.p;
+  PP.mat_off = d_mat_off_.p;
+  PP.mat = d_mat_.p;
+  PP.scratch = d_scratch_.p;
+  PP.scratch_cap = d_scratch_.n;
+  PP.ctl = d_ctl_.p;
+  PP.top_k = cfg_.top_k;
+  PP.stats = d_stats_.p;
+  PP.err = d_err_.p;
+  PrepareKernel<<<1, kPrepThreads, sizeof(PrepSmem), stream_>>>(PP);
+  int cnt = 0;
+  CheckCuda(cudaMemcpyAsync(&cnt, d_cand_cnt_.p, sizeof(int), cudaMemcpyDeviceToHost, stream_), "d2h");
+  CheckCuda(cudaStreamSynchronize(stream_), "prepare sync");
+  CheckError();
+  std::vector<int2> h(static_cast<size_t>(cnt));
+  if (cnt > 0) {
+    CheckCuda(cudaMemcpy(h.data(), d_cand_.p, sizeof(int2) * static_cast<size_t>(cnt), cudaMemcpyDeviceToHost),
+              "d2h cand");
+  }
+  for (int i = 0; i < cnt && i < cap; ++i) {
+    a_idx[i] = h[static_cast<size_t>(i)].x;
+    b_idx[i] = h[static_cast<size_t>(i)].y;
+  }
+  n_groups_ = -1;
+  return cnt;
+}
+
+void Engine::MergePairs(const int32_t* keep, const int32_t* remove, int64_t count) {
+  if (count <= 0) return;
+  std::vector<char> seen(static_cast<size_t>(n_), 0);
+  for (int64_t i = 0; i < count; ++i) {
+    const int k = keep[i], r = remove[i];
+    if (k < 0 || r < 0 || k >= n_ || r >= n_ || k == r) throw std::invalid_argument("invalid merge endpoints");
+    if (seen[static_cast<size_t>(k)] || seen[static_cast<size_t>(r)]) {
+      throw std::invalid_argument("merge batch requires endpoint-disjoint pairs");
+    }
+    seen[static_cast<size_t>(k)] = 1;
+    seen[static_cast<size_t>(r)] = 1;
+  }
+  EnsurePoolRoom();
+  // one pseudo-group holding the whole batch
+  n_groups_ = 1;
+  h_glen_.assign(1, 0);
+  PrepareIterationBuffers();
+  d_sel_keep_.ensure(static_cast<size_t>(count));
+  d_sel_rem_.ensure(static_cast<size_t>(count));
+  d_sel_gain_.ensure(static_cast<size_t>(count));
+  d_sel_ok_.ensure(static_cast<size_t>(count));
+  const long long zero = 0;
+  const int cnt = static_cast<int>(count);
+  CheckCuda(cudaMemcpyAsync(d_sel_off_.p, &zero, sizeof(long long), cudaMemcpyHostToDevice, stream_), "h2d");
+  CheckCuda(cudaMemcpyAsync(d_sel_cnt_.p, &cnt, sizeof(int), cudaMemcpyHostToDevice, stream_), "h2d");
+  CheckCuda(cudaMemcpyAsync(d_sel_keep_.p, keep, sizeof(int) * static_cast<size_t>(count), cudaMemcpyHostToDevice,
+                            stream_), "h2d");
+  CheckCuda(cudaMemcpyAsync(d_sel_rem_.p, remove, sizeof(int) * static_cast<size_t>(count), cudaMemcpyHostToDevice,
+                            stream_), "h2d");
+  CheckCuda(cudaMemsetAsync(d_sel_gain_.p, 0, sizeof(long long) * static_cast<size_t>(count), stream_), "memset");
+  CheckCuda(cudaMemsetAsync(d_sel_ok_.p, 1, static_cast<size_t>(count), stream_), "memset");
+  ++block_stamp_;
+  CheckCuda(cudaMemsetAsync(d_ctl_.p, 0, sizeof(BlockCtl), stream_), "memset ctl");
+  LaunchCommit(0, 1, false);
+  RelabelKernel<<<(n_ + 255) / 256, 256, 0, stream_>>>(d_label_.p, d_fwd_.p, n_);
+  n_groups_ = -1;
+  CheckCuda(cudaStreamSynchronize(stream_), "merge pairs sync");
+  CheckError();
+}
+
+}  // namespace beam

@@ -1,0 +1,229 @@
+"""Python face of the GB300 merge loop, mirroring the reference's Sweg /
+QuotientGraph operations (src/sweg.cpp, src/quotient_graph.cpp) over the C ABI.
+
+    g = Graph.generate("rmat:scale=19,ef=2,a=0.57,b=0.19,c=0.19,seed=7")
+    e = Engine(g, ea_use_threshold=True)
+    e.run(20)                       # Sweg::Run
+    labels, head, nxt = e.partition()
+    enc = g.encode(head, nxt)       # Sweg::Encode + compression metrics
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native as N
+
+__all__ = ["Graph", "Engine", "EngineOptions"]
+
+
+def _ptr(a: np.ndarray, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))
+
+
+class Graph:
+    """Symmetric CSR graph held by the native library (reference loader rules)."""
+
+    def __init__(self, handle: int):
+        if not handle:
+            raise N.BeamError(N.lib().beam_graph_last_error().decode())
+        self._h = handle
+        L = N.lib()
+        self.n = int(L.beam_graph_num_nodes(handle))
+        self.edges = int(L.beam_graph_num_edges(handle))
+        self.arcs = int(L.beam_graph_num_arcs(handle))
+        self.row_ptr = np.ctypeslib.as_array(L.beam_graph_row_ptr(handle), shape=(self.n + 1,)).copy()
+        self.col_idx = (np.ctypeslib.as_array(L.beam_graph_col_idx(handle), shape=(self.arcs,)).copy()
+                        if self.arcs else np.zeros(0, np.int32))
+
+    @classmethod
+    def generate(cls, spec: str) -> "Graph":
+        return cls(N.lib().beam_graph_generate(spec.encode()))
+
+    @classmethod
+    def load_text(cls, path: str) -> "Graph":
+        return cls(N.lib().beam_graph_load_text(str(path).encode()))
+
+    @classmethod
+    def load_binary(cls, path: str) -> "Graph":
+        return cls(N.lib().beam_graph_load_binary(str(path).encode()))
+
+    @classmethod
+    def from_edges(cls, u, v) -> "Graph":
+        u = np.ascontiguousarray(u, dtype=np.int32)
+        v = np.ascontiguousarray(v, dtype=np.int32)
+        return cls(N.lib().beam_graph_from_edges(_ptr(u, C.c_int32), _ptr(v, C.c_int32), len(u)))
+
+    def edge_list(self) -> tuple[np.ndarray, np.ndarray]:
+        L = N.lib()
+        u = np.ctypeslib.as_array(L.beam_graph_edge_u(self._h), shape=(self.edges,)).copy()
+        v = np.ctypeslib.as_array(L.beam_graph_edge_v(self._h), shape=(self.edges,)).copy()
+        return u, v
+
+    def write_text(self, path: str) -> None:
+        N.check(N.lib().beam_graph_write_text(self._h, str(path).encode()), "beam_graph_last_error")
+
+    def write_binary(self, path: str) -> None:
+        N.check(N.lib().beam_graph_write_binary(self._h, str(path).encode()), "beam_graph_last_error")
+
+    def encode(self, head: np.ndarray, nxt: np.ndarray, out_dir: str | None = None) -> dict:
+        enc = N.Encoding()
+        head = np.ascontiguousarray(head, np.int32)
+        nxt = np.ascontiguousarray(nxt, np.int32)
+        N.check(N.lib().beam_encode(self.n, self.arcs, _ptr(self.row_ptr, C.c_int64), _ptr(self.col_idx, C.c_int32),
+                                    _ptr(head, C.c_int32), _ptr(nxt, C.c_int32),
+                                    None if out_dir is None else str(out_dir).encode(), C.byref(enc)),
+                "beam_encode_last_error")
+        return enc.as_dict()
+
+    def exact_partition_cost(self, labels: np.ndarray) -> int:
+        labels = np.ascontiguousarray(labels, np.int32)
+        out = C.c_int64()
+        N.check(N.lib().beam_exact_partition_cost(self.n, _ptr(self.row_ptr, C.c_int64),
+                                                  _ptr(self.col_idx, C.c_int32), _ptr(labels, C.c_int32),
+                                                  C.byref(out)), "beam_encode_last_error")
+        return int(out.value)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            N.lib().beam_graph_free(h)
+            self._h = None
+
+
+def partition_hash(labels: np.ndarray) -> int:
+    labels = np.ascontiguousarray(labels, np.int32)
+    return int(N.lib().beam_partition_hash(len(labels), _ptr(labels, C.c_int32)))
+
+
+@dataclass
+class EngineOptions:
+    top_k: int = 16
+    group_batch_size: int = 64
+    divide_hash_dims: int = 16
+    divide_max_group: int = 512
+    ea_use_threshold: bool = True
+    seed: int = 1
+    device: int = 0
+
+
+class Engine:
+    """Device-resident merge loop for one graph (one GPU)."""
+
+    def __init__(self, graph: Graph, options: EngineOptions | None = None, **kw):
+        o = options or EngineOptions(**kw)
+        cfg = N.EngineConfig()
+        N.lib().beam_engine_default_config(C.byref(cfg))
+        cfg.top_k, cfg.group_batch_size = o.top_k, o.group_batch_size
+        cfg.divide_hash_dims, cfg.divide_max_group = o.divide_hash_dims, o.divide_max_group
+        cfg.ea_use_threshold, cfg.seed, cfg.device = int(o.ea_use_threshold), o.seed, o.device
+        h = C.c_void_p()
+        N.check(N.lib().beam_engine_create(graph.n, graph.arcs, _ptr(graph.row_ptr, C.c_int64),
+                                           _ptr(graph.col_idx, C.c_int32), C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.n = graph.n
+        self.options = o
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            N.lib().beam_engine_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # Sweg::Run / Divide / Merge
+    def reset(self) -> None:
+        N.check(N.lib().beam_engine_reset(self._h))
+
+    def run(self, iterations: int = 20) -> None:
+        N.check(N.lib().beam_engine_run(self._h, iterations))
+
+    def divide(self, iteration: int) -> None:
+        N.check(N.lib().beam_engine_divide(self._h, iteration))
+
+    def merge(self, iteration: int, total: int = 20) -> None:
+        N.check(N.lib().beam_engine_merge(self._h, iteration, total))
+
+    def groups(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        na, ng = C.c_int64(), C.c_int64()
+        N.check(N.lib().beam_engine_group_counts(self._h, C.byref(na), C.byref(ng)))
+        order = np.zeros(max(na.value, 1), np.int32)
+        starts = np.zeros(max(ng.value, 1), np.int32)
+        lengths = np.zeros(max(ng.value, 1), np.int32)
+        N.check(N.lib().beam_engine_groups(self._h, _ptr(order, C.c_int32), _ptr(starts, C.c_int32),
+                                           _ptr(lengths, C.c_int32)))
+        return order[:na.value], starts[:ng.value], lengths[:ng.value]
+
+    def score_pairs(self, a, b) -> tuple[np.ndarray, np.ndarray]:
+        a = np.ascontiguousarray(a, np.int32)
+        b = np.ascontiguousarray(b, np.int32)
+        gain = np.zeros(len(a), np.int64)
+        before = np.zeros(len(a), np.int64)
+        N.check(N.lib().beam_engine_score_pairs(self._h, _ptr(a, C.c_int32), _ptr(b, C.c_int32), len(a),
+                                                _ptr(gain, C.c_int64), _ptr(before, C.c_int64)))
+        return gain, before
+
+    def prepare_group(self, q) -> np.ndarray:
+        q = np.ascontiguousarray(q, np.int32)
+        cap = max(1, len(q) * max(1, self.options.top_k))
+        a = np.zeros(cap, np.int32)
+        b = np.zeros(cap, np.int32)
+        cnt = C.c_int64()
+        N.check(N.lib().beam_engine_prepare_group(self._h, _ptr(q, C.c_int32), len(q), _ptr(a, C.c_int32),
+                                                  _ptr(b, C.c_int32), cap, C.byref(cnt)))
+        return np.stack([a[:cnt.value], b[:cnt.value]], axis=1)
+
+    def merge_pairs(self, keep, remove) -> None:
+        keep = np.ascontiguousarray(keep, np.int32)
+        remove = np.ascontiguousarray(remove, np.int32)
+        N.check(N.lib().beam_engine_merge_pairs(self._h, _ptr(keep, C.c_int32), _ptr(remove, C.c_int32),
+                                                len(keep)))
+
+    def partition(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        labels = np.zeros(self.n, np.int32)
+        head = np.zeros(self.n, np.int32)
+        nxt = np.zeros(self.n, np.int32)
+        N.check(N.lib().beam_engine_partition(self._h, _ptr(labels, C.c_int32), _ptr(head, C.c_int32),
+                                              _ptr(nxt, C.c_int32)))
+        return labels, head, nxt
+
+    def row(self, rep: int) -> tuple[np.ndarray, np.ndarray, int, int]:
+        """(neighbours, counts, size, internal) of one supernode's quotient row."""
+        ln, size, internal = C.c_int64(), C.c_int64(), C.c_int64()
+        N.check(N.lib().beam_engine_export_row(self._h, rep, None, None, 0, C.byref(ln), C.byref(size),
+                                               C.byref(internal)))
+        nb = np.zeros(max(ln.value, 1), np.int32)
+        cnt = np.zeros(max(ln.value, 1), np.int64)
+        N.check(N.lib().beam_engine_export_row(self._h, rep, _ptr(nb, C.c_int32), _ptr(cnt, C.c_int64), ln.value,
+                                               C.byref(ln), C.byref(size), C.byref(internal)))
+        return nb[:ln.value], cnt[:ln.value], int(size.value), int(internal.value)
+
+    def stats(self) -> dict:
+        st = N.EngineStats()
+        N.check(N.lib().beam_engine_get_stats(self._h, C.byref(st)))
+        return st.as_dict()
+
+    def quotient_nnz(self) -> int:
+        out = C.c_int64()
+        N.check(N.lib().beam_engine_quotient_nnz(self._h, C.byref(out)))
+        return int(out.value)
+
+    def set_timed_kernel(self, which: int) -> None:
+        N.check(N.lib().beam_engine_set_timed_kernel(self._h, which))
+
+    def timed_kernel(self) -> tuple[float, int]:
+        ms, launches = C.c_double(), C.c_int64()
+        N.check(N.lib().beam_engine_timed_kernel(self._h, C.byref(ms), C.byref(launches)))
+        return float(ms.value), int(launches.value)
+
+    def synchronize(self) -> None:
+        N.check(N.lib().beam_engine_synchronize(self._h))

@@ -77,6 +77,98 @@ const int32_t* beam_graph_edge_v(const beam_graph* g);
 void beam_graph_free(beam_graph* g);
 const char* beam_graph_last_error(void);
 
+/* ---------------------------------------------------------------- engine */
+
+typedef struct beam_engine beam_engine;
+
+/* Flags of the recommended mode (src/main.cpp:14-56 defaults in brackets). */
+typedef struct {
+  int32_t top_k;             /* --top-k [16] */
+  int32_t group_batch_size;  /* --group-batch-size [64] */
+  int32_t divide_hash_dims;  /* --divide-hash-dims [16] */
+  int32_t divide_max_group;  /* --divide-max-group [512], at most 1024 */
+  int32_t ea_use_threshold;  /* --ea-use-threshold (reciprocal policy) */
+  int32_t device;            /* CUDA device ordinal */
+  uint64_t seed;             /* --seed [1] */
+} beam_engine_config;
+
+/* Counters with the reference's metric names (include/sweg.hpp:221-386). */
+typedef struct {
+  double runtime_run_ms, runtime_divide_ms, runtime_merge_ms;
+  uint64_t merge_group_count, merge_group_max_size, merge_raw_pair_count;
+  uint64_t merge_candidate_pairs_after_prune, candidate_proxy_pairs_examined;
+  uint64_t merge_exact_gain_calls, exact_gain_input_nnz;
+  uint64_t exact_raw_entries_a, exact_raw_entries_b, exact_union_neighbors, exact_overlap_neighbors;
+  uint64_t merge_positive_gain_pairs, merge_rejected_by_threshold, merge_rejected_by_overlap;
+  uint64_t merge_candidate_pairs, merge_selected_pairs, merge_total_local_gain;
+  uint64_t selected_merges_for_validation, validation_exact_calls, validation_exact_row_entry_work;
+  uint64_t accepted_merges_after_validation, rejected_nonpositive, update_touched_quotient_entries;
+  uint64_t isolated_gain_sum, divide_max_group_size, divide_fallback_splits;
+  /* this implementation's own counters */
+  uint64_t rows_rewritten, row_entries_rewritten;
+  uint64_t score_bytes, prepare_bytes, update_bytes, divide_bytes; /* algorithmic HBM bytes */
+  uint64_t blocks, iterations, pool_compactions, active_supernodes, groups_last;
+} beam_engine_stats;
+
+/* Kernel classes for beam_engine_set_timed_kernel. */
+enum { BEAM_TIME_NONE = 0, BEAM_TIME_SCORE = 1, BEAM_TIME_PREPARE = 2, BEAM_TIME_UPDATE = 3, BEAM_TIME_DIVIDE = 4 };
+
+void beam_engine_default_config(beam_engine_config* cfg);
+/* Uploads the HOST CSR (row_ptr[n+1], col_idx[arcs], sorted rows, no loops)
+ * to the device and builds the singleton quotient graph. */
+int beam_engine_create(int32_t n, int64_t arcs, const int64_t* row_ptr, const int32_t* col_idx,
+                       const beam_engine_config* cfg, beam_engine** out);
+void beam_engine_destroy(beam_engine* e);
+/* Back to the singleton partition, rebuilt from the resident CSR. */
+int beam_engine_reset(beam_engine* e);
+int beam_engine_run(beam_engine* e, int32_t iterations);
+int beam_engine_divide(beam_engine* e, int32_t iter);
+int beam_engine_merge(beam_engine* e, int32_t iter, int32_t total_iterations);
+/* Divide output: active reps in group order, group starts and lengths. */
+int beam_engine_group_counts(beam_engine* e, int64_t* n_active, int64_t* n_groups);
+int beam_engine_groups(beam_engine* e, int32_t* order, int32_t* starts, int32_t* lengths);
+/* Exact merge gain and before-cost for explicit pairs of active reps. */
+int beam_engine_score_pairs(beam_engine* e, const int32_t* rep_a, const int32_t* rep_b, int64_t count,
+                            int64_t* gain, int64_t* before);
+/* EA-proxy candidates (a_idx < b_idx, sorted) of one explicit group; the
+ * Divide output is consumed (call beam_engine_divide again before merging). */
+int beam_engine_prepare_group(beam_engine* e, const int32_t* q, int32_t g, int32_t* a_idx, int32_t* b_idx,
+                              int64_t cap, int64_t* count);
+/* Applies endpoint-disjoint merges (keep, remove) as one batch. */
+int beam_engine_merge_pairs(beam_engine* e, const int32_t* keep, const int32_t* remove, int64_t count);
+/* node -> rep labels, head[rep] (-1 when inactive) and next[node] member lists. */
+int beam_engine_partition(beam_engine* e, int32_t* labels, int32_t* head, int32_t* next);
+int beam_engine_export_row(beam_engine* e, int32_t rep, int32_t* nb, int64_t* cnt, int64_t cap, int64_t* len,
+                           int64_t* size, int64_t* internal);
+int beam_engine_get_stats(beam_engine* e, beam_engine_stats* out);
+/* QuotientGraph::Nnz (src/quotient_graph.cpp:259-270). */
+int beam_engine_quotient_nnz(beam_engine* e, int64_t* nnz);
+/* CUDA-event timing of every launch of one kernel class (BEAM_TIME_*). */
+int beam_engine_set_timed_kernel(beam_engine* e, int32_t which);
+int beam_engine_timed_kernel(beam_engine* e, double* ms, int64_t* launches);
+int beam_engine_synchronize(beam_engine* e);
+const char* beam_engine_last_error(void);
+
+/* ------------------------------------------------------- summary output */
+
+typedef struct {
+  int64_t supernodes, p, cp, cm, superedges_loop, superedges_nonloop;
+  int64_t encoding_cost_standard, encoding_cost_mags_x2;
+  double cost_ratio_standard, cost_ratio_mags_compatible;
+} beam_encoding;
+
+/* Sweg::Encode (mags-compatible) of the partition given as member lists
+ * (head[rep] = -1 for inactive reps, next[node]), plus the compression
+ * metrics; writes G.txt, P.txt, Cp.txt, Cm.txt into out_dir when not NULL. */
+int beam_encode(int32_t n, int64_t arcs, const int64_t* row_ptr, const int32_t* col_idx, const int32_t* head,
+                const int32_t* next, const char* out_dir, beam_encoding* out);
+/* CostOracle::ExactPartitionCost of a node -> label partition. */
+int beam_exact_partition_cost(int32_t n, const int64_t* row_ptr, const int32_t* col_idx, const int32_t* labels,
+                              int64_t* cost);
+/* Sweg::PartitionHash: FNV-1a over the node -> rep labels. */
+uint64_t beam_partition_hash(int32_t n, const int32_t* labels);
+const char* beam_encode_last_error(void);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

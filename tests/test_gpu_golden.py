@@ -1,0 +1,48 @@
+"""End-to-end parity of the GPU merge loop with the reference program: every
+fixture in tests/golden/golden.json (made by the reference itself) must give
+the same partition hash, the same counters and byte-identical
+G.txt / P.txt / Cp.txt / Cm.txt (integer work: bit-exact)."""
+
+import pytest
+
+from conftest import file_hashes, golden_cases, graph_for, iterations_from_flags, options_from_flags
+
+pytestmark = pytest.mark.gpu
+
+COUNTERS = ["merge_group_count", "merge_group_max_size", "merge_raw_pair_count",
+            "merge_candidate_pairs_after_prune", "candidate_proxy_pairs_examined", "merge_exact_gain_calls",
+            "exact_gain_input_nnz", "exact_raw_entries_a", "exact_raw_entries_b", "exact_union_neighbors",
+            "exact_overlap_neighbors", "merge_positive_gain_pairs", "merge_rejected_by_threshold",
+            "merge_rejected_by_overlap", "merge_candidate_pairs", "merge_selected_pairs", "merge_total_local_gain",
+            "isolated_gain_sum", "selected_merges_for_validation", "validation_exact_calls",
+            "validation_exact_row_entry_work", "accepted_merges_after_validation", "rejected_nonpositive",
+            "update_touched_quotient_entries", "divide_max_group_size", "divide_fallback_splits"]
+
+
+def gpu_metrics(case, tmp_path):
+    from beam_gb300 import Engine, partition_hash
+    g = graph_for(case)
+    with Engine(g, **options_from_flags(case["flags"])) as e:
+        e.run(iterations_from_flags(case["flags"]))
+        labels, head, nxt = e.partition()
+        st = e.stats()
+        qnnz = e.quotient_nnz()
+    enc = g.encode(head, nxt, tmp_path)
+    m = {k: st[k] for k in COUNTERS}
+    m.update(n=g.n, partition_hash=partition_hash(labels), exact_partition_cost=g.exact_partition_cost(labels),
+             supernode_count=enc["supernodes"], P=enc["p"], Cp=enc["cp"], Cm=enc["cm"],
+             num_superedges_loop=enc["superedges_loop"], num_superedges_nonloop=enc["superedges_nonloop"],
+             encoding_cost_mags_x2=enc["encoding_cost_mags_x2"],
+             cost_ratio_mags_compatible=f"{enc['cost_ratio_mags_compatible']:.6f}", quotient_nnz_final=qnnz)
+    return {k: str(v) for k, v in m.items()}, enc
+
+
+@pytest.mark.parametrize("case", golden_cases(), ids=lambda c: c["name"])
+def test_gpu_matches_reference(case, tmp_path):
+    got, enc = gpu_metrics(case, tmp_path)
+    want = case["metrics"]
+    diffs = {k: (want[k], got[k]) for k in got if k in want and want[k] != got[k]}
+    assert not diffs, diffs
+    # payload cost == exact partition cost (src/main.cpp:561-566)
+    assert int(got["exact_partition_cost"]) * 2 == enc["encoding_cost_mags_x2"]
+    assert file_hashes(tmp_path) == case["files_sha256"]
