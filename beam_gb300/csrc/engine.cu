@@ -156,7 +156,7 @@ Engine::Engine(int n, int64_t arcs, const int64_t* row_ptr, const int32_t* col_i
   d_qcap_.ensure(un);
   d_qsize_.ensure(un);
   d_qint_.ensure(un);
-  for (DevBuf<int>* b : {&d_label_, &d_head_, &d_next_, &d_tail_, &d_fwd_, &d_stamp_, &d_partner_, &d_claim_,
+  for (DevBuf<int>* b : {&d_label_, &d_head_, &d_next_, &d_tail_, &d_fwd_, &d_stamp_, &d_partner_, &d_claim_, &d_seq_,
                          &d_order_, &d_order_alt_, &d_head_flag_, &d_vals_, &d_vals_alt_, &d_need_, &d_seg_beg_,
                          &d_seg_end_, &d_pos_map_, &d_gstart_, &d_glen_, &d_group_of_, &d_idx_in_group_,
                          &d_acc_keep_, &d_acc_rem_, &d_aff_}) {
@@ -187,7 +187,7 @@ Engine::~Engine() {
   d_qcap_.release();
   d_qsize_.release();
   d_qint_.release();
-  for (DevBuf<int>* b : {&d_label_, &d_head_, &d_next_, &d_tail_, &d_fwd_, &d_stamp_, &d_partner_, &d_claim_,
+  for (DevBuf<int>* b : {&d_label_, &d_head_, &d_next_, &d_tail_, &d_fwd_, &d_stamp_, &d_partner_, &d_claim_, &d_seq_,
                          &d_order_, &d_order_alt_, &d_head_flag_, &d_vals_, &d_vals_alt_, &d_need_, &d_seg_beg_,
                          &d_seg_end_, &d_pos_map_, &d_gstart_, &d_glen_, &d_group_of_, &d_idx_in_group_,
                          &d_acc_keep_, &d_acc_rem_, &d_aff_, &d_counts_, &d_cand_cnt_, &d_sel_keep_, &d_sel_rem_,

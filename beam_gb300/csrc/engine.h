@@ -162,7 +162,7 @@ class Engine {
 
   // partition
   DevBuf<int> d_label_, d_head_, d_next_, d_tail_, d_fwd_;
-  DevBuf<int> d_stamp_, d_partner_, d_claim_;
+  DevBuf<int> d_stamp_, d_partner_, d_claim_, d_seq_;
 
   // divide
   DevBuf<int> d_order_, d_order_alt_, d_head_flag_;

@@ -726,6 +726,7 @@ struct CommitParams {
   int* fwd;
   int* stamp;
   int* partner;
+  int* seq;
   int* claim;
   int block_stamp;
   int* acc_keep;
@@ -739,6 +740,12 @@ struct CommitParams {
 // Commit-time validation: ExactMergeGainPersistent of each selected pair
 // against the block-start state; accepted iff gain > 0. The scored gain was
 // computed on the same state, so a difference is an internal error.
+//
+// Then the endpoints of every accepted pair are marked for this block: stamp
+// (keep / remove), partner, and the pair's position in commit order (group
+// order, then selection order), which the reference's sequential Update_S
+// calls follow. Without check_gain (explicit merge batches) all pairs are
+// accepted and only marked.
 __global__ void __launch_bounds__(256) ValidateKernel(CommitParams P) {
   const int gid = P.g0 + blockIdx.x;
   const int cnt = P.sel_cnt[gid];
@@ -748,16 +755,27 @@ __global__ void __launch_bounds__(256) ValidateKernel(CommitParams P) {
   for (int s = warp; s < cnt; s += 8) {
     const int k = P.sel_keep[so + s];
     const int r = P.sel_rem[so + s];
-    long long gain = 0, before = 0;
-    GainWork w = {0, 0, 0, 0};
-    WarpExactGain(P.Q, k, r, &gain, &before, &w, P.err);
-    if (lane == 0) {
-      if (P.check_gain && gain != P.sel_gain[so + s]) RaiseError(P.err, kErrValidation, k, r, 0);
-      P.sel_ok[so + s] = gain > 0 ? 1 : 0;
-      atomicAdd(&P.stats[kStValidationCalls], 1ull);
-      atomicAdd(&P.stats[kStValidationWork], static_cast<unsigned long long>(w.raw_a + w.raw_b));
-      atomicAdd(&P.stats[kStIsolatedGain], static_cast<unsigned long long>(P.sel_gain[so + s]));
-      if (gain <= 0) atomicAdd(&P.stats[kStRejNonpositive], 1ull);
+    bool ok = true;
+    if (P.check_gain) {
+      long long gain = 0, before = 0;
+      GainWork w = {0, 0, 0, 0};
+      WarpExactGain(P.Q, k, r, &gain, &before, &w, P.err);
+      ok = gain > 0;
+      if (lane == 0) {
+        if (gain != P.sel_gain[so + s]) RaiseError(P.err, kErrValidation, k, r, 0);
+        P.sel_ok[so + s] = ok ? 1 : 0;
+        atomicAdd(&P.stats[kStValidationCalls], 1ull);
+        atomicAdd(&P.stats[kStValidationWork], static_cast<unsigned long long>(w.raw_a + w.raw_b));
+        atomicAdd(&P.stats[kStIsolatedGain], static_cast<unsigned long long>(P.sel_gain[so + s]));
+        if (!ok) atomicAdd(&P.stats[kStRejNonpositive], 1ull);
+      }
+    }
+    if (lane == 0 && ok) {
+      P.stamp[k] = 2 * P.block_stamp;
+      P.stamp[r] = 2 * P.block_stamp + 1;
+      P.partner[k] = r;
+      P.partner[r] = k;
+      P.seq[r] = static_cast<int>(so + s);
     }
   }
 }
@@ -765,6 +783,12 @@ __global__ void __launch_bounds__(256) ValidateKernel(CommitParams P) {
 // Update_S for the accepted pairs: sizes, internal counts, member lists,
 // forwarding; records the block's merges and claims every neighbour row of a
 // removed supernode for the row pass.
+//
+// QuotientGraph::Merge reports 2 + 3 * |row(remove)| touched entries, with
+// the row as it stands when that merge runs in commit order: every earlier
+// merge (k', r') of the block whose r' and k' are both neighbours of remove
+// has folded r' into k' there, one entry fewer. The count below replays that
+// from the block-start row.
 __global__ void __launch_bounds__(256) ApplyKernel(CommitParams P) {
   const int gid = P.g0 + blockIdx.x;
   const int cnt = P.sel_cnt[gid];
@@ -772,12 +796,24 @@ __global__ void __launch_bounds__(256) ApplyKernel(CommitParams P) {
   const int lane = threadIdx.x & 31;
   const long long so = P.sel_off[gid];
   const QuotientView& Q = P.Q;
+  const int remove_stamp = 2 * P.block_stamp + 1;
   for (int s = warp; s < cnt; s += 8) {
     if (!P.sel_ok[so + s]) continue;
     const int k = P.sel_keep[so + s];
     const int r = P.sel_rem[so + s];
     const Entry* rr = Q.ent + Q.off[r];
     const int lr = Q.len[r];
+    const int my_seq = static_cast<int>(so + s);
+    int folded = 0;
+    for (int i = lane; i < lr; i += 32) {
+      const int x = EntNb(rr[i]);
+      if (x == k) continue;
+      if (P.stamp[x] == remove_stamp && P.seq[x] < my_seq && RowLookup(rr, lr, P.partner[x]) != 0) ++folded;
+      if (atomicExch(&P.claim[x], P.block_stamp) != P.block_stamp) {
+        P.aff[atomicAdd(&P.ctl->aff_cnt, 1u)] = x;
+      }
+    }
+    folded = WarpSumInt(folded);
     if (lane == 0) {
       const long long ekr = RowLookup(Q.ent + Q.off[k], Q.len[k], r);
       Q.internal[k] += Q.internal[r] + ekr;
@@ -788,22 +824,12 @@ __global__ void __launch_bounds__(256) ApplyKernel(CommitParams P) {
       P.tail[k] = P.tail[r];
       P.head[r] = -1;
       P.fwd[r] = k;
-      P.stamp[k] = 2 * P.block_stamp;
-      P.stamp[r] = 2 * P.block_stamp + 1;
-      P.partner[k] = r;
-      P.partner[r] = k;
       const unsigned idx = atomicAdd(&P.ctl->acc_cnt, 1u);
       P.acc_keep[idx] = k;
       P.acc_rem[idx] = r;
       atomicAdd(&P.stats[kStAccepted], 1ull);
-      atomicAdd(&P.stats[kStTouched], static_cast<unsigned long long>(2 + 3 * (lr - (ekr > 0 ? 1 : 0))));
-    }
-    for (int i = lane; i < lr; i += 32) {
-      const int x = EntNb(rr[i]);
-      if (x == k) continue;
-      if (atomicExch(&P.claim[x], P.block_stamp) != P.block_stamp) {
-        P.aff[atomicAdd(&P.ctl->aff_cnt, 1u)] = x;
-      }
+      atomicAdd(&P.stats[kStTouched],
+                static_cast<unsigned long long>(2 + 3 * (lr - (ekr > 0 ? 1 : 0) - folded)));
     }
   }
 }
@@ -1106,6 +1132,7 @@ void Engine::LaunchCommit(int64_t g0, int nbg, bool check_gain) {
   C.fwd = d_fwd_.p;
   C.stamp = d_stamp_.p;
   C.partner = d_partner_.p;
+  C.seq = d_seq_.p;
   C.claim = d_claim_.p;
   C.block_stamp = block_stamp_;
   C.acc_keep = d_acc_keep_.p;
@@ -1114,7 +1141,7 @@ void Engine::LaunchCommit(int64_t g0, int nbg, bool check_gain) {
   C.ctl = d_ctl_.p;
   C.stats = d_stats_.p;
   C.err = d_err_.p;
-  if (check_gain) ValidateKernel<<<nbg, 256, 0, stream_>>>(C);
+  ValidateKernel<<<nbg, 256, 0, stream_>>>(C);
   ApplyKernel<<<nbg, 256, 0, stream_>>>(C);
   RowsParams R;
   R.Q = View();

@@ -151,7 +151,7 @@ def test_hub_rows_and_large_groups():
         if a != b:
             u.append(int(min(a, b)))
             v.append(int(max(a, b)))
-    pairs = sorted(set(zip(u, v)))
+    pairs = sorted({(min(a, b), max(a, b)) for a, b in zip(u, v)})  # each undirected edge once
     g = Graph.from_edges([p[0] for p in pairs], [p[1] for p in pairs])
     e = Engine(g)
     o = Oracle.from_graph(g)
