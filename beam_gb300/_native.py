@@ -27,6 +27,8 @@ class EngineConfig(C.Structure):
         ("ea_use_threshold", i32),
         ("device", i32),
         ("seed", u64),
+        ("verify_cuda_gain", i32),
+        ("reserved0", i32),
     ]
 
 
@@ -105,6 +107,10 @@ SIGNATURES = {
     "beam_engine_set_timed_kernel": (C.c_int, [vp, i32]),
     "beam_engine_timed_kernel": (C.c_int, [vp, P_f64, P_i64]),
     "beam_engine_synchronize": (C.c_int, [vp]),
+    "beam_engine_step_timer_start": (C.c_int, [vp]),
+    "beam_engine_step_timer_stop": (C.c_int, [vp, P_f64]),
+    "beam_engine_flush_l2": (C.c_int, [vp]),
+    "beam_engine_launch_count": (C.c_int, [vp, P_i64]),
     "beam_engine_last_error": (C.c_char_p, []),
     "beam_encode": (C.c_int, [i32, i64, P_i64, P_i32, P_i32, P_i32, C.c_char_p, C.POINTER(Encoding)]),
     "beam_exact_partition_cost": (C.c_int, [i32, P_i64, P_i32, P_i32, P_i64]),

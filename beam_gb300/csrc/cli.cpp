@@ -43,6 +43,7 @@ struct Options {
   int divide_max_group = 512;
   bool ea_use_threshold = false;
   bool write_output = false;
+  bool verify_cuda_gain = false;
   bool show_help = false;
   double error_bound = 0.0;
   uint64_t seed = 1;
@@ -104,9 +105,8 @@ Options ParseArgs(int argc, char** argv) {
     else if (a == "--device" && has) o.device = std::stoi(take());
     else if (a == "--ea-use-threshold") o.ea_use_threshold = true;
     else if (a == "--write-output") o.write_output = true;
-    else if (a == "--verify-cuda-gain") {
-      // every commit re-scores its pairs on the device and checks them
-    } else {
+    else if (a == "--verify-cuda-gain") o.verify_cuda_gain = true;  // re-score and check every commit
+    else {
       std::cerr << "Unknown or incomplete argument: " << a << "\n";
       o.show_help = true;
       return o;
@@ -180,6 +180,7 @@ int Run(int argc, char** argv) {
   cfg.ea_use_threshold = o.ea_use_threshold ? 1 : 0;
   cfg.seed = o.seed;
   cfg.device = o.device;
+  cfg.verify_cuda_gain = o.verify_cuda_gain ? 1 : 0;
   beam_engine* e = nullptr;
   if (beam_engine_create(static_cast<int32_t>(n), arcs, beam_graph_row_ptr(g), beam_graph_col_idx(g), &cfg, &e) != 0) {
     throw std::runtime_error(beam_engine_last_error());

@@ -217,9 +217,11 @@ void Engine::Divide(int iter) {
   };
 
   // Active supernodes in ascending id order.
+  ++launches_;
   ActiveFlagsKernel<<<Blocks(n, T), T, 0, s>>>(d_qsize_.p, n, flags);
   scan_excl(flags, scan, n);
   CheckCuda(cudaMemsetAsync(d_head_flag_.p, 0, sizeof(int) * static_cast<size_t>(n), s), "memset");
+  ++launches_;
   ScatterActiveKernel<<<Blocks(n, T), T, 0, s>>>(d_qsize_.p, scan, n, d_order_.p, d_head_flag_.p);
   int last_scan = 0, last_flag = 0;
   fetch2(scan + n - 1, flags + n - 1, &last_scan, &last_flag);
@@ -241,10 +243,12 @@ void Engine::Divide(int iter) {
     for (int depth = 0; depth <= cfg_.divide_hash_dims; ++depth) {
       const bool fallback = depth == cfg_.divide_hash_dims;
       scan_incl(d_head_flag_.p, scan, count);
+      ++launches_;
       SegStartsKernel<<<Blocks(count, T), T, 0, s>>>(d_head_flag_.p, scan, count, seg_start);
       int seg_total = 0, dummy = 0;
       fetch2(scan + count - 1, scan + count - 1, &seg_total, &dummy);
       segs = seg_total;
+      ++launches_;
       SegLenKernel<<<Blocks(segs, T), T, 0, s>>>(seg_start, segs, count, cfg_.divide_max_group, seg_len, unf_flag,
                                                  unf_len);
       scan_excl(unf_flag, unf_idx, segs);
@@ -256,20 +260,24 @@ void Engine::Divide(int iter) {
       int items_last = 0, items_len = 0;
       fetch2(unf_off + segs - 1, unf_len + segs - 1, &items_last, &items_len);
       const int items = items_last + items_len;
+      ++launches_;
       CompactItemsKernel<<<Blocks(count, T), T, 0, s>>>(scan, seg_start, seg_len, unf_flag, unf_idx, unf_off, count,
                                                         d_pos_map_.p, item_seg, ubeg, uend);
       if (fallback) {
         hstats_.divide_fallback_splits += static_cast<uint64_t>(nu);
       } else {
         ++need_stamp_;
+        ++launches_;
         MarkNeedKernel<<<Blocks(items, T), T, 0, s>>>(d_order_.p, d_pos_map_.p, items, d_need_.p, need_stamp_,
                                                       d_hash_.p);
         const uint64_t base = HashRankBase(cfg_.seed, dim_order[static_cast<size_t>(depth)], iter);
         BeginTimed(kTimeDivide);
+        ++launches_;
         MinHashKernel<<<152 * 8, 256, 0, s>>>(d_arc_src_.p, d_col_.p, d_label_.p, d_need_.p, arcs_, n,
                                               need_stamp_, base, d_hash_.p);
         EndTimed(kTimeDivide);
       }
+      ++launches_;
       GatherKeysKernel<<<Blocks(items, T), T, 0, s>>>(d_order_.p, d_pos_map_.p, items, d_hash_.p, fallback ? 1 : 0,
                                                       cfg_.seed, iter, d_keys_.p, d_vals_.p);
       size_t bytes = 0;
@@ -280,18 +288,22 @@ void Engine::Divide(int iter) {
       CheckCuda(cub::DeviceSegmentedSort::StableSortPairs(d_cub_tmp_.p, bytes, d_keys_.p, d_keys_alt_.p, d_vals_.p,
                                                           d_vals_alt_.p, items, nu, ubeg, uend, s),
                 "cub segmented sort");
+      ++launches_;
       ScatterSortedKernel<<<Blocks(items, T), T, 0, s>>>(d_pos_map_.p, item_seg, ubeg, items, d_keys_alt_.p,
                                                          d_vals_alt_.p, fallback ? 1 : 0, cfg_.divide_max_group,
                                                          d_order_.p, d_head_flag_.p);
     }
     // final segments are the groups
     scan_incl(d_head_flag_.p, scan, count);
+    ++launches_;
     SegStartsKernel<<<Blocks(count, T), T, 0, s>>>(d_head_flag_.p, scan, count, seg_start);
     int seg_total = 0, dummy = 0;
     fetch2(scan + count - 1, scan + count - 1, &seg_total, &dummy);
     segs = seg_total;
+    ++launches_;
     SegLenKernel<<<Blocks(segs, T), T, 0, s>>>(seg_start, segs, count, cfg_.divide_max_group, seg_len, unf_flag,
                                                unf_len);
+    ++launches_;
     GroupInfoKernel<<<Blocks(count, T), T, 0, s>>>(d_order_.p, scan, seg_start, seg_len, count, d_group_of_.p,
                                                    d_idx_in_group_.p, d_stats_.p);
     CheckCuda(cudaMemcpyAsync(d_gstart_.p, seg_start, sizeof(int) * static_cast<size_t>(segs),

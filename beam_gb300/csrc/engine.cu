@@ -176,6 +176,10 @@ Engine::Engine(int n, int64_t arcs, const int64_t* row_ptr, const int32_t* col_i
 
 Engine::~Engine() {
   for (cudaEvent_t e : ev_pool_) cudaEventDestroy(e);
+  for (cudaEvent_t e : step_ev_) {
+    if (e) cudaEventDestroy(e);
+  }
+  d_flush_.release();
   if (stream_) cudaStreamSynchronize(stream_);
   for (auto* b : {&d_pool_[0], &d_pool_[1]}) b->release();
   d_rowptr_.release();
@@ -217,9 +221,11 @@ Engine::~Engine() {
 void Engine::Reset() {
   const int T = 256;
   cur_pool_ = 0;
+  ++launches_;
   InitScalarsKernel<<<(n_ + T - 1) / T, T, 0, stream_>>>(n_, d_qsize_.p, d_qint_.p, d_label_.p, d_head_.p,
                                                           d_next_.p, d_tail_.p, d_fwd_.p, d_stamp_.p, d_partner_.p,
                                                           d_claim_.p, d_need_.p);
+  ++launches_;
   InitRowsKernel<<<152 * 16, 256, 0, stream_>>>(d_rowptr_.p, d_col_.p, n_, d_pool_[0].p, d_qoff_.p, d_qlen_.p,
                                                 d_qcap_.p, d_arc_src_.p);
   const unsigned long long top = static_cast<unsigned long long>(arcs_);
@@ -270,6 +276,7 @@ void Engine::CompactPool() {
   DevBuf<long long> lens, offs;
   lens.ensure(static_cast<size_t>(n_) + 1);
   offs.ensure(static_cast<size_t>(n_) + 1);
+  ++launches_;
   LenToLongKernel<<<(n_ + T - 1) / T, T, 0, stream_>>>(d_qlen_.p, d_qsize_.p, n_, lens.p);
   size_t bytes = 0;
   CheckCuda(cub::DeviceScan::ExclusiveSum(nullptr, bytes, lens.p, offs.p, n_ + 1, stream_), "scan size");
@@ -277,6 +284,7 @@ void Engine::CompactPool() {
   CheckCuda(cudaMemsetAsync(lens.p + n_, 0, sizeof(long long), stream_), "memset");
   CheckCuda(cub::DeviceScan::ExclusiveSum(d_cub_tmp_.p, bytes, lens.p, offs.p, n_ + 1, stream_), "scan");
   const int dst = 1 - cur_pool_;
+  ++launches_;
   CompactRowsKernel<<<152 * 16, 256, 0, stream_>>>(d_pool_[cur_pool_].p, d_pool_[dst].p, offs.p, d_qoff_.p,
                                                    d_qlen_.p, d_qcap_.p, d_qsize_.p, n_);
   CheckCuda(cudaMemcpyAsync(d_pool_top_.p, offs.p + n_, sizeof(long long), cudaMemcpyDeviceToDevice, stream_),
@@ -364,6 +372,7 @@ int64_t Engine::QuotientNnz() {
   const int T = 256;
   lens.ensure(static_cast<size_t>(n_));
   sum.ensure(1);
+  ++launches_;
   LenToLongKernel<<<(n_ + T - 1) / T, T, 0, stream_>>>(d_qlen_.p, d_qsize_.p, n_, lens.p);
   size_t bytes = 0;
   CheckCuda(cub::DeviceReduce::Sum(nullptr, bytes, lens.p, sum.p, n_, stream_), "reduce size");
@@ -408,6 +417,28 @@ void Engine::EndTimed(int which) {
   CheckCuda(cudaEventRecord(ev_pool_[ev_used_ + 1], stream_), "event record");
   ev_used_ += 2;
   ++timed_launches_;
+}
+
+void Engine::StepTimerStart() {
+  for (cudaEvent_t& e : step_ev_) {
+    if (!e) CheckCuda(cudaEventCreate(&e), "cudaEventCreate");
+  }
+  CheckCuda(cudaEventRecord(step_ev_[0], stream_), "event record");
+}
+
+double Engine::StepTimerStopMs() {
+  CheckCuda(cudaEventRecord(step_ev_[1], stream_), "event record");
+  CheckCuda(cudaEventSynchronize(step_ev_[1]), "event sync");
+  float ms = 0.f;
+  CheckCuda(cudaEventElapsedTime(&ms, step_ev_[0], step_ev_[1]), "event elapsed");
+  return ms;
+}
+
+void Engine::FlushL2() {
+  const size_t bytes = static_cast<size_t>(256) << 20;  // twice the 129 MB L2 of a GB300
+  d_flush_.ensure(bytes);
+  CheckCuda(cudaMemsetAsync(d_flush_.p, static_cast<int>(launches_ & 0xff), bytes, stream_), "l2 flush");
+  CheckCuda(cudaStreamSynchronize(stream_), "sync");
 }
 
 double Engine::TimedKernelMs() {
@@ -462,6 +493,8 @@ void beam_engine_default_config(beam_engine_config* cfg) {
   cfg->ea_use_threshold = 1;
   cfg->device = 0;
   cfg->seed = 1;
+  cfg->verify_cuda_gain = 0;
+  cfg->reserved0 = 0;
 }
 
 int beam_engine_create(int32_t n, int64_t arcs, const int64_t* row_ptr, const int32_t* col_idx,
@@ -478,6 +511,7 @@ int beam_engine_create(int32_t n, int64_t arcs, const int64_t* row_ptr, const in
       c.ea_use_threshold = cfg->ea_use_threshold != 0;
       c.seed = cfg->seed;
       c.device = cfg->device;
+      c.verify_cuda_gain = cfg->verify_cuda_gain != 0;
     }
     auto* e = new beam_engine{new Engine(n, arcs, row_ptr, col_idx, c)};
     *out = e;
@@ -603,6 +637,18 @@ int beam_engine_timed_kernel(beam_engine* e, double* ms, int64_t* launches) {
 }
 
 int beam_engine_synchronize(beam_engine* e) { return Guard([&] { e->impl->Synchronize(); }); }
+
+int beam_engine_step_timer_start(beam_engine* e) { return Guard([&] { e->impl->StepTimerStart(); }); }
+
+int beam_engine_step_timer_stop(beam_engine* e, double* ms) {
+  return Guard([&] { *ms = e->impl->StepTimerStopMs(); });
+}
+
+int beam_engine_flush_l2(beam_engine* e) { return Guard([&] { e->impl->FlushL2(); }); }
+
+int beam_engine_launch_count(beam_engine* e, int64_t* launches) {
+  return Guard([&] { *launches = e->impl->launches(); });
+}
 
 }  // extern "C"
 

@@ -22,6 +22,8 @@ struct EngineConfig {
   bool ea_use_threshold = true;
   uint64_t seed = 1;
   int device = 0;
+  // Re-score every selected pair at commit and check it (--verify-cuda-gain).
+  bool verify_cuda_gain = false;
 };
 
 // Largest group the kernels accept (bounded by the packed select keys and
@@ -125,19 +127,26 @@ class Engine {
   double TimedKernelMs();
   int64_t TimedKernelLaunches() const { return timed_launches_; }
   void Synchronize();
+  // Step timing with CUDA events on the engine stream.
+  void StepTimerStart();
+  double StepTimerStopMs();
+  // Writes a buffer larger than the L2 cache on the engine stream.
+  void FlushL2();
+  // Number of this library's kernels launched since creation.
+  int64_t launches() const { return launches_; }
 
  private:
   void CheckError();
   void InitQuotient();
   void EnsurePoolRoom();
   void CompactPool();
-  void RunBlock(int64_t g0, int64_t g1, int64_t max_cap, double threshold);
+  void RunBlock(int rg0, int rg1, double threshold);
   void PrepareIterationBuffers();
   void BeginTimed(int which);
   void EndTimed(int which);
   void ConfigureKernels();
   QuotientView View();
-  void LaunchCommit(int64_t g0, int nbg, bool check_gain);
+  void LaunchCommit(int rg0, int nrg, int64_t max_pairs, bool verify);
 
   int n_;
   int64_t arcs_;
@@ -190,12 +199,20 @@ class Engine {
   DevBuf<unsigned long long> d_stats_;
   DevBuf<DevError> d_err_;
   std::vector<int> h_glen_;
+  std::vector<int> h_real_;      // Divide ids of the groups with >= 2 members
+  std::vector<int> h_block_rg_;  // per 64-group block: first real-group position
+  DevBuf<int> d_real_;
   std::vector<long long> h_cand_off_, h_sel_off_, h_mat_off_;
   PinnedBuf<long long> h_pin_;
   int block_stamp_ = 0;
   int64_t n_active_ = 0;
   int64_t n_groups_ = 0;
   HostStats hstats_;
+
+  // launch accounting and step timing
+  int64_t launches_ = 0;
+  cudaEvent_t step_ev_[2] = {nullptr, nullptr};
+  DevBuf<unsigned char> d_flush_;
 
   // kernel timing
   int timed_kind_ = kTimeNone;

@@ -6,13 +6,12 @@
 //                   (QuotientGraph::ExactMergeGainPersistentImpl, src/quotient_graph.cpp:340-462)
 //   SelectKernel    reciprocal threshold filter + g0 greedy selection
 //                   (src/sweg.cpp:2146-2186, 2188-2281)
-//   ValidateKernel  commit-time exact gain against the block-start state
-//                   (CommitSelectedPairs, src/sweg.cpp:2683-2719)
-//   ApplyKernel     Update_S bookkeeping: sizes, internal counts, member lists
-//                   (src/sweg.cpp:2977-3015, src/quotient_graph.cpp:628-648)
-//   RowsKernel      quotient rows after the block's merges: keep rows rebuilt
-//                   from keep+remove, neighbour rows of removed supernodes
-//                   rewritten in place (src/quotient_graph.cpp:651-719)
+//   CommitKernel    CommitSelectedPairs + Update_S + QuotientGraph::Merge for
+//                   the block (src/sweg.cpp:2665-2769, 2977-3015,
+//                   src/quotient_graph.cpp:628-742): sizes, internal counts,
+//                   member lists, keep rows rebuilt from keep+remove, neighbour
+//                   rows of removed supernodes rewritten in place
+//   VerifyKernel    optional commit-time re-scoring (--verify-cuda-gain)
 //
 // The reference validates every selected pair of a block before applying any
 // of them (Update_S runs after the validation loop), and the pairs of a block
@@ -38,6 +37,7 @@ constexpr int kSelectThreads = 512;
 constexpr int kSelectSmemKeys = 8192;
 constexpr int kRowsThreads = 256;
 constexpr int kRowSmem = 2048;       // staged row entries in shared memory
+constexpr int kClaimSmem = 4096;     // claimed neighbour rows listed in shared memory
 constexpr int kKeyIdxBits = 10;      // a_idx, b_idx < kMaxGroup
 constexpr long long kKeyGainMax = (1ll << (64 - 2 * kKeyIdxBits)) - 1;
 
@@ -135,6 +135,10 @@ __device__ void WarpExactGain(const QuotientView& Q, int a, int b, long long* ga
 
 // ------------------------------------------------------------ prepare
 
+// Per-group arrays of the merge kernels (cand_off, cand_cnt, mat_off,
+// sel_off, sel_cnt) are indexed by the group's position in the iteration's
+// list of groups with at least two members ("real" groups); real[ri] is the
+// Divide group id. A block covers the real groups [rg0, rg0 + nrg).
 struct PrepareParams {
   QuotientView Q;
   const int* order;
@@ -142,7 +146,8 @@ struct PrepareParams {
   const int* glen;
   const int* group_of;
   const int* idx_in_group;
-  int g0;
+  const int* real;
+  int rg0;
   const long long* cand_off;
   int2* cand;
   int* cand_cnt;
@@ -201,16 +206,17 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
   const int lane = tid & 31;
   const int warp = tid >> 5;
   const int nwarps = kPrepThreads / 32;
-  const int gid = P.g0 + blockIdx.x;
+  const int ri = P.rg0 + blockIdx.x;
+  const int gid = P.real[ri];
   const int g = P.glen[gid];
   if (g < 2) {
-    if (tid == 0) P.cand_cnt[gid] = 0;
+    if (tid == 0) P.cand_cnt[ri] = 0;
     return;
   }
   if (g > kMaxGroup) {
     if (tid == 0) {
       RaiseError(P.err, kErrGroupTooLarge, gid, g, 0);
-      P.cand_cnt[gid] = 0;
+      P.cand_cnt[ri] = 0;
     }
     return;
   }
@@ -258,7 +264,7 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
     }
     __syncthreads();
     if (big == nullptr) {
-      if (tid == 0) P.cand_cnt[gid] = 0;
+      if (tid == 0) P.cand_cnt[ri] = 0;
       return;
     }
     unsigned char* b = reinterpret_cast<unsigned char*>(big);
@@ -272,7 +278,7 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
   for (unsigned h = tid; h <= hmask; h += kPrepThreads) heads[h] = -1;
   // per-group pair tables
   const long long gg = static_cast<long long>(g) * g;
-  unsigned char* mat = P.mat + P.mat_off[gid];
+  unsigned char* mat = P.mat + P.mat_off[ri];
   long long* pmat = reinterpret_cast<long long*>(mat);
   double* rmat = reinterpret_cast<double*>(mat + 8 * gg);
   int* cmat = reinterpret_cast<int*>(mat + 16 * gg);
@@ -455,7 +461,7 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
     __syncthreads();
   }
   const int nc = carry;
-  int2* out = P.cand + P.cand_off[gid];
+  int2* out = P.cand + P.cand_off[ri];
   for (int a = warp; a < g; a += nwarps) {
     int pos = S.eoff[a];
     for (int base = a + 1; base < g; base += 32) {
@@ -467,7 +473,7 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
     }
   }
   if (tid == 0) {
-    P.cand_cnt[gid] = nc;
+    P.cand_cnt[ri] = nc;
     atomicAdd(&P.stats[kStGroupCount], 1ull);
     atomicMax(&P.stats[kStGroupMaxSize], static_cast<unsigned long long>(g));
     atomicAdd(&P.stats[kStRawPairCount], static_cast<unsigned long long>(g) * (g - 1) / 2);
@@ -484,7 +490,9 @@ struct ScoreParams {
   QuotientView Q;
   const int* order;
   const int* gstart;
-  int g0;
+  const int* real;
+  int rg0;
+  int nrg;
   const long long* cand_off;
   const int2* cand;
   const int* cand_cnt;
@@ -508,26 +516,37 @@ __device__ __forceinline__ void FlushScoreStats(unsigned long long* stats, const
             static_cast<unsigned long long>(8 * (w.raw_a + w.raw_b) + 4 * w.uni + 24 * pairs));
 }
 
+// Index of the real group owning a slot: last ri in [lo, hi) with off[ri] <= slot.
+__device__ __forceinline__ int OwnerOfSlot(const long long* off, int lo, int hi, long long slot) {
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= slot) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+// One warp per candidate slot of the block (the concatenated per-group
+// candidate capacities); slots past a group's candidate count are skipped.
 __global__ void __launch_bounds__(kScoreThreads) ScoreKernel(ScoreParams P) {
-  const int gid = P.g0 + blockIdx.x;
-  const int cnt = P.cand_cnt[gid];
-  const int p0 = blockIdx.y * kPairsPerScoreCta;
-  if (p0 >= cnt) return;
-  const int p1 = min(cnt, p0 + kPairsPerScoreCta);
-  const int warp = threadIdx.x >> 5;
+  const long long s0 = P.cand_off[P.rg0];
+  const long long s1 = P.cand_off[P.rg0 + P.nrg];
   const int lane = threadIdx.x & 31;
-  const long long base = P.cand_off[gid];
-  const int* q = P.order + P.gstart[gid];
+  const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
   GainWork w = {0, 0, 0, 0};
   long long pairs = 0, view_nnz = 0;
-  for (int p = p0 + warp; p < p1; p += kScoreThreads / 32) {
-    const int2 c = P.cand[base + p];
+  for (long long slot = s0 + warp; slot < s1; slot += nw) {
+    const int ri = OwnerOfSlot(P.cand_off, P.rg0, P.rg0 + P.nrg, slot);
+    const int p = static_cast<int>(slot - P.cand_off[ri]);
+    if (p >= P.cand_cnt[ri]) continue;
+    const int* q = P.order + P.gstart[P.real[ri]];
+    const int2 c = P.cand[slot];
     const int a = q[c.x];
     const int b = q[c.y];
     long long gain = 0, before = 0;
     WarpExactGain(P.Q, a, b, &gain, &before, &w, P.err);
     if (lane == 0) {
-      P.res[base + p] = make_longlong2(gain, before);
+      P.res[slot] = make_longlong2(gain, before);
       ++pairs;
       view_nnz += P.Q.len[a] + (P.Q.internal[a] > 0 ? 1 : 0) + P.Q.len[b] + (P.Q.internal[b] > 0 ? 1 : 0);
     }
@@ -564,7 +583,8 @@ struct SelectParams {
   const int* order;
   const int* gstart;
   const int* glen;
-  int g0;
+  const int* real;
+  int rg0;
   const long long* cand_off;
   const int2* cand;
   const int* cand_cnt;
@@ -574,6 +594,11 @@ struct SelectParams {
   int* sel_rem;
   long long* sel_gain;
   int* sel_cnt;
+  const int* qlen;
+  int* stamp;
+  int* partner;
+  int* seq;
+  int block_stamp;
   double threshold;
   int use_threshold;
   unsigned char* scratch;
@@ -604,6 +629,12 @@ __device__ void CtaBitonicSort(unsigned long long* keys, int n) {
   }
 }
 
+// Threshold filter, g0 order (gain desc, a_idx asc, b_idx asc) by a bitonic
+// sort of packed keys, greedy endpoint-disjoint pass. The selected pairs are
+// the block's commit list: the reference validates each against the same
+// block-start state its score came from (gain > 0 by the filter), so every
+// one is accepted; their endpoints are marked here (stamp, partner, commit
+// order) for the commit kernel.
 __global__ void __launch_bounds__(kSelectThreads) SelectKernel(SelectParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned long long* skeys = reinterpret_cast<unsigned long long*>(smem_raw);
@@ -612,11 +643,12 @@ __global__ void __launch_bounds__(kSelectThreads) SelectKernel(SelectParams P) {
   __shared__ unsigned long long* gkeys;
   __shared__ unsigned long long rej_thr, positive;
   const int tid = threadIdx.x;
-  const int gid = P.g0 + blockIdx.x;
+  const int ri = P.rg0 + blockIdx.x;
+  const int gid = P.real[ri];
   const int g = P.glen[gid];
-  const int cnt = g >= 2 && g <= kMaxGroup ? P.cand_cnt[gid] : 0;
+  const int cnt = g >= 2 && g <= kMaxGroup ? P.cand_cnt[ri] : 0;
   if (cnt == 0) {
-    if (tid == 0) P.sel_cnt[gid] = 0;
+    if (tid == 0) P.sel_cnt[ri] = 0;
     return;
   }
   int cap = 1;
@@ -632,10 +664,10 @@ __global__ void __launch_bounds__(kSelectThreads) SelectKernel(SelectParams P) {
   __syncthreads();
   unsigned long long* keys = gkeys;
   if (keys == nullptr) {
-    if (tid == 0) P.sel_cnt[gid] = 0;
+    if (tid == 0) P.sel_cnt[ri] = 0;
     return;
   }
-  const long long base = P.cand_off[gid];
+  const long long base = P.cand_off[ri];
   unsigned long long my_rej = 0, my_pos = 0;
   for (int c = tid; c < cnt; c += kSelectThreads) {
     const longlong2 r = P.res[base + c];
@@ -675,10 +707,10 @@ __global__ void __launch_bounds__(kSelectThreads) SelectKernel(SelectParams P) {
   if (m > 1) CtaBitonicSort(keys, pow2);
   if (tid == 0) {
     const int* q = P.order + P.gstart[gid];
-    const long long so = P.sel_off[gid];
+    const long long so = P.sel_off[ri];
     int ns = 0;
     long long total = 0;
-    unsigned long long overlap = 0;
+    unsigned long long overlap = 0, work = 0;
     const unsigned long long idx_mask = (1ull << kKeyIdxBits) - 1;
     for (int k = 0; k < m; ++k) {
       const unsigned long long key = keys[k];
@@ -691,19 +723,32 @@ __global__ void __launch_bounds__(kSelectThreads) SelectKernel(SelectParams P) {
       }
       used[a] = 1;
       used[b] = 1;
-      P.sel_keep[so + ns] = q[a];
-      P.sel_rem[so + ns] = q[b];
+      const int keep = q[a];
+      const int rem = q[b];
+      P.sel_keep[so + ns] = keep;
+      P.sel_rem[so + ns] = rem;
       P.sel_gain[so + ns] = gain;
+      P.stamp[keep] = 2 * P.block_stamp;
+      P.stamp[rem] = 2 * P.block_stamp + 1;
+      P.partner[keep] = rem;
+      P.partner[rem] = keep;
+      P.seq[rem] = static_cast<int>(so + ns);
+      work += static_cast<unsigned long long>(P.qlen[keep] + P.qlen[rem]);
       ++ns;
       total += gain;
     }
-    P.sel_cnt[gid] = ns;
+    P.sel_cnt[ri] = ns;
     atomicAdd(&P.stats[kStRejThreshold], rej_thr);
     atomicAdd(&P.stats[kStPositive], positive);
     atomicAdd(&P.stats[kStRejOverlap], overlap);
     atomicAdd(&P.stats[kStCandPairs], static_cast<unsigned long long>(m));
     atomicAdd(&P.stats[kStSelected], static_cast<unsigned long long>(ns));
     atomicAdd(&P.stats[kStLocalGain], static_cast<unsigned long long>(total));
+    // CommitSelectedPairs validation counters (src/sweg.cpp:2683-2719): one
+    // exact-gain call per selected pair, reading both rows, all accepted.
+    atomicAdd(&P.stats[kStValidationCalls], static_cast<unsigned long long>(ns));
+    atomicAdd(&P.stats[kStValidationWork], work);
+    atomicAdd(&P.stats[kStIsolatedGain], static_cast<unsigned long long>(total));
   }
 }
 
@@ -711,14 +756,13 @@ __global__ void __launch_bounds__(kSelectThreads) SelectKernel(SelectParams P) {
 
 struct CommitParams {
   QuotientView Q;
-  int g0;
+  int rg0;
+  int nrg;
   const long long* sel_off;
   const int* sel_keep;
   const int* sel_rem;
   const long long* sel_gain;
   const int* sel_cnt;
-  unsigned char* sel_ok;
-  int check_gain;
   // Update_S state
   int* head;
   int* next;
@@ -729,134 +773,53 @@ struct CommitParams {
   int* seq;
   int* claim;
   int block_stamp;
-  int* acc_keep;
-  int* acc_rem;
-  int* aff;
-  BlockCtl* ctl;
-  unsigned long long* stats;
-  DevError* err;
-};
-
-// Commit-time validation: ExactMergeGainPersistent of each selected pair
-// against the block-start state; accepted iff gain > 0. The scored gain was
-// computed on the same state, so a difference is an internal error.
-//
-// Then the endpoints of every accepted pair are marked for this block: stamp
-// (keep / remove), partner, and the pair's position in commit order (group
-// order, then selection order), which the reference's sequential Update_S
-// calls follow. Without check_gain (explicit merge batches) all pairs are
-// accepted and only marked.
-__global__ void __launch_bounds__(256) ValidateKernel(CommitParams P) {
-  const int gid = P.g0 + blockIdx.x;
-  const int cnt = P.sel_cnt[gid];
-  const int warp = threadIdx.x >> 5;
-  const int lane = threadIdx.x & 31;
-  const long long so = P.sel_off[gid];
-  for (int s = warp; s < cnt; s += 8) {
-    const int k = P.sel_keep[so + s];
-    const int r = P.sel_rem[so + s];
-    bool ok = true;
-    if (P.check_gain) {
-      long long gain = 0, before = 0;
-      GainWork w = {0, 0, 0, 0};
-      WarpExactGain(P.Q, k, r, &gain, &before, &w, P.err);
-      ok = gain > 0;
-      if (lane == 0) {
-        if (gain != P.sel_gain[so + s]) RaiseError(P.err, kErrValidation, k, r, 0);
-        P.sel_ok[so + s] = ok ? 1 : 0;
-        atomicAdd(&P.stats[kStValidationCalls], 1ull);
-        atomicAdd(&P.stats[kStValidationWork], static_cast<unsigned long long>(w.raw_a + w.raw_b));
-        atomicAdd(&P.stats[kStIsolatedGain], static_cast<unsigned long long>(P.sel_gain[so + s]));
-        if (!ok) atomicAdd(&P.stats[kStRejNonpositive], 1ull);
-      }
-    }
-    if (lane == 0 && ok) {
-      P.stamp[k] = 2 * P.block_stamp;
-      P.stamp[r] = 2 * P.block_stamp + 1;
-      P.partner[k] = r;
-      P.partner[r] = k;
-      P.seq[r] = static_cast<int>(so + s);
-    }
-  }
-}
-
-// Update_S for the accepted pairs: sizes, internal counts, member lists,
-// forwarding; records the block's merges and claims every neighbour row of a
-// removed supernode for the row pass.
-//
-// QuotientGraph::Merge reports 2 + 3 * |row(remove)| touched entries, with
-// the row as it stands when that merge runs in commit order: every earlier
-// merge (k', r') of the block whose r' and k' are both neighbours of remove
-// has folded r' into k' there, one entry fewer. The count below replays that
-// from the block-start row.
-__global__ void __launch_bounds__(256) ApplyKernel(CommitParams P) {
-  const int gid = P.g0 + blockIdx.x;
-  const int cnt = P.sel_cnt[gid];
-  const int warp = threadIdx.x >> 5;
-  const int lane = threadIdx.x & 31;
-  const long long so = P.sel_off[gid];
-  const QuotientView& Q = P.Q;
-  const int remove_stamp = 2 * P.block_stamp + 1;
-  for (int s = warp; s < cnt; s += 8) {
-    if (!P.sel_ok[so + s]) continue;
-    const int k = P.sel_keep[so + s];
-    const int r = P.sel_rem[so + s];
-    const Entry* rr = Q.ent + Q.off[r];
-    const int lr = Q.len[r];
-    const int my_seq = static_cast<int>(so + s);
-    int folded = 0;
-    for (int i = lane; i < lr; i += 32) {
-      const int x = EntNb(rr[i]);
-      if (x == k) continue;
-      if (P.stamp[x] == remove_stamp && P.seq[x] < my_seq && RowLookup(rr, lr, P.partner[x]) != 0) ++folded;
-      if (atomicExch(&P.claim[x], P.block_stamp) != P.block_stamp) {
-        P.aff[atomicAdd(&P.ctl->aff_cnt, 1u)] = x;
-      }
-    }
-    folded = WarpSumInt(folded);
-    if (lane == 0) {
-      const long long ekr = RowLookup(Q.ent + Q.off[k], Q.len[k], r);
-      Q.internal[k] += Q.internal[r] + ekr;
-      Q.internal[r] = 0;
-      Q.size[k] += Q.size[r];
-      Q.size[r] = 0;
-      P.next[P.tail[k]] = P.head[r];
-      P.tail[k] = P.tail[r];
-      P.head[r] = -1;
-      P.fwd[r] = k;
-      const unsigned idx = atomicAdd(&P.ctl->acc_cnt, 1u);
-      P.acc_keep[idx] = k;
-      P.acc_rem[idx] = r;
-      atomicAdd(&P.stats[kStAccepted], 1ull);
-      atomicAdd(&P.stats[kStTouched],
-                static_cast<unsigned long long>(2 + 3 * (lr - (ekr > 0 ? 1 : 0) - folded)));
-    }
-  }
-}
-
-// ------------------------------------------------------------ rows
-
-struct RowsParams {
-  QuotientView Q;
-  const int* stamp;
-  const int* partner;
-  int block_stamp;
-  const int* acc_keep;
-  const int* acc_rem;
-  const int* aff;
-  BlockCtl* ctl;
   unsigned long long* pool_top;
   unsigned long long pool_cap;
   unsigned char* scratch;
   unsigned long long scratch_cap;
+  BlockCtl* ctl;
   unsigned long long* stats;
   DevError* err;
 };
+
+// Optional re-validation (--verify-cuda-gain): recomputes the exact gain of
+// every selected pair against the block-start state and checks it equals
+// the scored gain and is positive.
+__global__ void __launch_bounds__(256) VerifyKernel(CommitParams P) {
+  const long long s0 = P.sel_off[P.rg0];
+  const long long s1 = P.sel_off[P.rg0 + P.nrg];
+  const int lane = threadIdx.x & 31;
+  const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
+  for (long long slot = s0 + warp; slot < s1; slot += nw) {
+    const int ri = OwnerOfSlot(P.sel_off, P.rg0, P.rg0 + P.nrg, slot);
+    if (slot - P.sel_off[ri] >= P.sel_cnt[ri]) continue;
+    const int k = P.sel_keep[slot];
+    const int r = P.sel_rem[slot];
+    long long gain = 0, before = 0;
+    WarpExactGain(P.Q, k, r, &gain, &before, nullptr, P.err);
+    if (lane == 0 && (gain != P.sel_gain[slot] || gain <= 0)) RaiseError(P.err, kErrValidation, k, r, 0);
+  }
+}
+
+// Marks the endpoints of an explicit merge batch (no selection step).
+__global__ void MarkKernel(const int* keep, const int* rem, int count, int* stamp, int* partner, int* seq,
+                           int block_stamp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) {
+    stamp[keep[i]] = 2 * block_stamp;
+    stamp[rem[i]] = 2 * block_stamp + 1;
+    partner[keep[i]] = rem[i];
+    partner[rem[i]] = keep[i];
+    seq[rem[i]] = i;
+  }
+}
 
 struct RowsSmem {
   Entry s[kRowSmem];
   int d[kRowSmem + 1];
   Entry ins[kRowSmem];
+  int claimed[kClaimSmem];
 };
 
 // Rewrites a staged sorted row S[0..L) (adjacent equal ids allowed: the keep
@@ -864,7 +827,7 @@ struct RowsSmem {
 // ids sk / sr are dropped, entries of supernodes removed in this block move
 // to their keep partner (summed into its entry, or inserted at its sorted
 // position). Returns the new length.
-__device__ int RewriteRow(const RowsParams& P, Entry* S, int L, int* D, Entry* INS, int sk, int sr, Entry* out) {
+__device__ int RewriteRow(const CommitParams& P, Entry* S, int L, int* D, Entry* INS, int sk, int sr, Entry* out) {
   using BlockScan = cub::BlockScan<int, kRowsThreads>;
   __shared__ typename BlockScan::TempStorage scan_tmp;
   __shared__ int nins, carry;
@@ -938,92 +901,154 @@ __device__ int RewriteRow(const RowsParams& P, Entry* S, int L, int* D, Entry* I
   return L - D[L] + m;
 }
 
-__global__ void __launch_bounds__(kRowsThreads) RowsKernel(RowsParams P) {
+// Staging buffers for a row of L entries: shared memory when it fits,
+// block scratch otherwise. Returns false (error raised) when scratch is out.
+__device__ bool StageBuffers(const CommitParams& P, RowsSmem& R, int L, Entry** S, int** D, Entry** INS) {
+  __shared__ Entry* gbuf;
+  if (L <= kRowSmem) {
+    *S = R.s;
+    *D = R.d;
+    *INS = R.ins;
+    return true;
+  }
+  int pow2 = 1;
+  while (pow2 < L) pow2 <<= 1;
+  if (threadIdx.x == 0) {
+    gbuf = reinterpret_cast<Entry*>(ScratchAlloc(P.scratch, P.scratch_cap, P.ctl,
+                                                 8ull * L + 4ull * (L + 1) + 8ull * pow2 + 512ull, P.err));
+  }
+  __syncthreads();
+  if (gbuf == nullptr) return false;
+  *S = gbuf;
+  *INS = gbuf + L;
+  *D = reinterpret_cast<int*>(gbuf + L + pow2);
+  return true;
+}
+
+// One CTA per selected pair of the block (persistent grid over the block's
+// selection slots). Per pair:
+//   Update_S bookkeeping: size, internal count, member list, forwarding, and
+//     QuotientGraph::Merge's touched-entry count replayed in commit order
+//   keep row <- merge(row keep, row remove) with the block's removes folded
+//     into their keeps, written to fresh pool space
+//   every neighbour row of remove that is not a keep/remove of this block is
+//     claimed once per block and rewritten in place (remove -> its keep)
+// Rows of keeps and removes are only read (the keep row goes to new space),
+// and a claimed neighbour row is touched by its claimant alone, so the CTAs
+// need no ordering among themselves.
+__global__ void __launch_bounds__(kRowsThreads) CommitKernel(CommitParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   RowsSmem& R = *reinterpret_cast<RowsSmem*>(smem_raw);
-  __shared__ Entry* gbuf;
   __shared__ long long new_off;
+  __shared__ int nclaimed, folded_sum;
+  __shared__ int* claim_buf;
   const QuotientView& Q = P.Q;
-  const int acc = static_cast<int>(P.ctl->acc_cnt);
-  const int total = acc + static_cast<int>(P.ctl->aff_cnt);
+  const long long s0 = P.sel_off[P.rg0];
+  const long long s1 = P.sel_off[P.rg0 + P.nrg];
   const int tid = threadIdx.x;
-  for (int w = blockIdx.x; w < total; w += gridDim.x) {
-    int sk = -1, sr = -1, row = -1;
-    if (w < acc) {
-      sk = P.acc_keep[w];
-      sr = P.acc_rem[w];
-    } else {
-      row = P.aff[w - acc];
-      if ((P.stamp[row] >> 1) == P.block_stamp) continue;  // keep/remove rows are rebuilt separately
+  const int remove_stamp = 2 * P.block_stamp + 1;
+  for (long long slot = s0 + blockIdx.x; slot < s1; slot += gridDim.x) {
+    const int ri = OwnerOfSlot(P.sel_off, P.rg0, P.rg0 + P.nrg, slot);
+    if (slot - P.sel_off[ri] >= P.sel_cnt[ri]) continue;
+    const int k = P.sel_keep[slot];
+    const int r = P.sel_rem[slot];
+    const Entry* rr = Q.ent + Q.off[r];
+    const Entry* rk = Q.ent + Q.off[k];
+    const int lr = Q.len[r];
+    const int lk = Q.len[k];
+    const int my_seq = static_cast<int>(slot);
+    if (tid == 0) {
+      nclaimed = 0;
+      folded_sum = 0;
+      claim_buf = lr <= kClaimSmem
+                      ? R.claimed
+                      : reinterpret_cast<int*>(ScratchAlloc(P.scratch, P.scratch_cap, P.ctl, 4ull * lr, P.err));
     }
-    const int L = w < acc ? Q.len[sk] + Q.len[sr] : Q.len[row];
-    Entry* S = R.s;
-    int* D = R.d;
-    Entry* INS = R.ins;
-    if (L > kRowSmem) {
-      int pow2 = 1;
-      while (pow2 < L) pow2 <<= 1;
-      if (tid == 0) {
-        gbuf = reinterpret_cast<Entry*>(ScratchAlloc(P.scratch, P.scratch_cap, P.ctl,
-                                                     8ull * L + 4ull * (L + 1) + 8ull * pow2 + 512ull, P.err));
-      }
-      __syncthreads();
-      if (gbuf == nullptr) return;
-      S = gbuf;
-      INS = S + L;
-      D = reinterpret_cast<int*>(INS + pow2);
+    __syncthreads();
+    if (claim_buf == nullptr) return;
+    // touched count and neighbour-row claims (block-start row of remove)
+    int folded = 0;
+    for (int i = tid; i < lr; i += kRowsThreads) {
+      const int x = EntNb(rr[i]);
+      if (x == k) continue;
+      const int sx = P.stamp[x];
+      if (sx == remove_stamp && P.seq[x] < my_seq && RowLookup(rr, lr, P.partner[x]) != 0) ++folded;
+      if ((sx >> 1) == P.block_stamp) continue;  // keep/remove rows are rebuilt by their own pair
+      if (atomicExch(&P.claim[x], P.block_stamp) != P.block_stamp) claim_buf[atomicAdd(&nclaimed, 1)] = x;
     }
-    if (w < acc) {
-      // stage merge(row k, row r): A entries before B entries on equal ids
-      const Entry* A = Q.ent + Q.off[sk];
-      const Entry* B = Q.ent + Q.off[sr];
-      const int la = Q.len[sk];
-      const int lb = Q.len[sr];
-      for (int i = tid; i < la; i += kRowsThreads) {
-        const Entry e = A[i];
-        S[i + RowLowerBound(B, lb, EntNb(e))] = e;
+    folded = WarpSumInt(folded);
+    if ((tid & 31) == 0 && folded) atomicAdd(&folded_sum, folded);
+    __syncthreads();
+    const int claimed = nclaimed;
+    // keep row <- merge(row k, row r), staged with keep entries first on ties
+    const int L = lk + lr;
+    Entry *S, *INS;
+    int* D;
+    if (!StageBuffers(P, R, L, &S, &D, &INS)) return;
+    for (int i = tid; i < lk; i += kRowsThreads) {
+      const Entry e = rk[i];
+      S[i + RowLowerBound(rr, lr, EntNb(e))] = e;
+    }
+    for (int j = tid; j < lr; j += kRowsThreads) {
+      const Entry e = rr[j];
+      const int key = EntNb(e);
+      int lo = 0, hi = lk;  // upper bound in row k
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (EntNb(rk[mid]) <= key) lo = mid + 1; else hi = mid;
       }
-      for (int j = tid; j < lb; j += kRowsThreads) {
-        const Entry e = B[j];
-        const int key = EntNb(e);
-        int lo = 0, hi = la;  // upper bound in A
-        while (lo < hi) {
-          const int mid = (lo + hi) >> 1;
-          if (EntNb(A[mid]) <= key) lo = mid + 1; else hi = mid;
-        }
-        S[j + lo] = e;
+      S[j + lo] = e;
+    }
+    if (tid == 0) {
+      const unsigned long long want = static_cast<unsigned long long>(L > 0 ? L : 1);
+      const unsigned long long at = atomicAdd(P.pool_top, want);
+      if (at + want > P.pool_cap) {
+        RaiseError(P.err, kErrPool, k, L, 0);
+        new_off = -1;
+      } else {
+        new_off = static_cast<long long>(at);
       }
-      if (tid == 0) {
-        const unsigned long long want = static_cast<unsigned long long>(L > 0 ? L : 1);
-        const unsigned long long at = atomicAdd(P.pool_top, want);
-        if (at + want > P.pool_cap) {
-          RaiseError(P.err, kErrPool, sk, L, 0);
-          new_off = -1;
-        } else {
-          new_off = static_cast<long long>(at);
-        }
-      }
+    }
+    __syncthreads();
+    if (new_off < 0) return;
+    const long long ekr = RowLookup(rk, lk, r);
+    const int nl = RewriteRow(P, S, L, D, INS, k, r, Q.ent + new_off);
+    if (tid == 0) {
+      Q.internal[k] += Q.internal[r] + ekr;
+      Q.internal[r] = 0;
+      Q.size[k] += Q.size[r];
+      Q.size[r] = 0;
+      P.next[P.tail[k]] = P.head[r];
+      P.tail[k] = P.tail[r];
+      P.head[r] = -1;
+      P.fwd[r] = k;
+      Q.off[k] = new_off;
+      Q.len[k] = nl;
+      Q.cap[k] = L > 0 ? L : 1;
+      Q.len[r] = 0;
+      atomicAdd(&P.stats[kStAccepted], 1ull);
+      atomicAdd(&P.stats[kStTouched],
+                static_cast<unsigned long long>(2 + 3 * (lr - (ekr > 0 ? 1 : 0) - folded_sum)));
+      atomicAdd(&P.stats[kStUpdateBytes], 8ull * (2ull * L + nl));
+    }
+    // neighbour rows claimed by this pair, rewritten in place
+    for (int c = 0; c < claimed; ++c) {
+      const int x = claim_buf[c];
+      Entry* rowp = Q.ent + Q.off[x];
+      const int lx = Q.len[x];
+      Entry *S2, *INS2;
+      int* D2;
+      if (!StageBuffers(P, R, lx, &S2, &D2, &INS2)) return;
+      for (int i = tid; i < lx; i += kRowsThreads) S2[i] = rowp[i];
       __syncthreads();
-      if (new_off < 0) return;
-      const int nl = RewriteRow(P, S, L, D, INS, sk, sr, Q.ent + new_off);
+      const int nlx = RewriteRow(P, S2, lx, D2, INS2, -1, -1, rowp);
       if (tid == 0) {
-        Q.off[sk] = new_off;
-        Q.len[sk] = nl;
-        Q.cap[sk] = L > 0 ? L : 1;
-        Q.len[sr] = 0;
-        atomicAdd(&P.stats[kStUpdateBytes], 8ull * (2ull * L + nl));
-      }
-    } else {
-      Entry* rowp = Q.ent + Q.off[row];
-      for (int i = tid; i < L; i += kRowsThreads) S[i] = rowp[i];
-      __syncthreads();
-      const int nl = RewriteRow(P, S, L, D, INS, -1, -1, rowp);
-      if (tid == 0) {
-        Q.len[row] = nl;
+        Q.len[x] = nlx;
         atomicAdd(&P.stats[kStRowsRewritten], 1ull);
-        atomicAdd(&P.stats[kStRowEntriesRewritten], static_cast<unsigned long long>(L));
-        atomicAdd(&P.stats[kStUpdateBytes], 8ull * (L + nl));
+        atomicAdd(&P.stats[kStRowEntriesRewritten], static_cast<unsigned long long>(lx));
+        atomicAdd(&P.stats[kStUpdateBytes], 8ull * (lx + nlx));
       }
+      __syncthreads();
     }
     __syncthreads();
   }
@@ -1052,54 +1077,69 @@ void Engine::ConfigureKernels() {
                                  static_cast<int>(sizeof(PrepSmem))), "prepare smem attribute");
   CheckCuda(cudaFuncSetAttribute(SelectKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  8 * kSelectSmemKeys), "select smem attribute");
-  CheckCuda(cudaFuncSetAttribute(RowsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(sizeof(RowsSmem))), "rows smem attribute");
+  CheckCuda(cudaFuncSetAttribute(CommitKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(sizeof(RowsSmem))), "commit smem attribute");
 }
 
+// Per-iteration layout: the groups with >= 2 members in Divide order, their
+// candidate / selection capacities (min(C(g,2), g*top_k) and g/2) as prefix
+// offsets, pair-table offsets restarting at every 64-group block, and for
+// every block the range of its real groups (empty blocks do no work).
 void Engine::PrepareIterationBuffers() {
   const int64_t G = n_groups_;
-  h_cand_off_.assign(static_cast<size_t>(G) + 1, 0);
-  h_sel_off_.assign(static_cast<size_t>(G) + 1, 0);
-  h_mat_off_.assign(static_cast<size_t>(G) + 1, 0);
-  long long max_mat = 0;
-  const long long k = cfg_.top_k > 0 ? cfg_.top_k : 1;
-  for (int64_t gi = 0; gi < G; ++gi) {
-    const long long g = h_glen_[static_cast<size_t>(gi)];
-    const long long pairs = g >= 2 ? std::min(g * (g - 1) / 2, g * k) : 0;
-    h_cand_off_[static_cast<size_t>(gi) + 1] = h_cand_off_[static_cast<size_t>(gi)] + pairs;
-    h_sel_off_[static_cast<size_t>(gi) + 1] = h_sel_off_[static_cast<size_t>(gi)] + (g >= 2 ? g / 2 : 0);
-  }
+  h_real_.clear();
+  h_block_rg_.clear();
   const int64_t bs = cfg_.group_batch_size;
+  const long long k = cfg_.top_k > 0 ? cfg_.top_k : 1;
   for (int64_t b0 = 0; b0 < G; b0 += bs) {
     const int64_t b1 = std::min(G, b0 + bs);
-    long long off = 0;
+    h_block_rg_.push_back(static_cast<int>(h_real_.size()));
     for (int64_t gi = b0; gi < b1; ++gi) {
-      const long long g = h_glen_[static_cast<size_t>(gi)];
-      h_mat_off_[static_cast<size_t>(gi)] = off;
-      if (g >= 2) off += (21 * g * g + 255) & ~255ll;
+      if (h_glen_[static_cast<size_t>(gi)] >= 2) h_real_.push_back(static_cast<int>(gi));
+    }
+  }
+  h_block_rg_.push_back(static_cast<int>(h_real_.size()));
+  const size_t R = h_real_.size();
+  h_cand_off_.assign(R + 1, 0);
+  h_sel_off_.assign(R + 1, 0);
+  h_mat_off_.assign(R + 1, 0);
+  long long max_mat = 0;
+  for (size_t ri = 0; ri < R; ++ri) {
+    const long long g = h_glen_[static_cast<size_t>(h_real_[ri])];
+    h_cand_off_[ri + 1] = h_cand_off_[ri] + std::min(g * (g - 1) / 2, g * k);
+    h_sel_off_[ri + 1] = h_sel_off_[ri] + g / 2;
+  }
+  for (size_t b = 0; b + 1 < h_block_rg_.size(); ++b) {
+    long long off = 0;
+    for (int ri = h_block_rg_[b]; ri < h_block_rg_[b + 1]; ++ri) {
+      const long long g = h_glen_[static_cast<size_t>(h_real_[static_cast<size_t>(ri)])];
+      h_mat_off_[static_cast<size_t>(ri)] = off;
+      off += (21 * g * g + 255) & ~255ll;
     }
     max_mat = std::max(max_mat, off);
   }
-  d_cand_off_.ensure(static_cast<size_t>(G) + 1);
-  d_sel_off_.ensure(static_cast<size_t>(G) + 1);
-  d_mat_off_.ensure(static_cast<size_t>(G) + 1);
-  d_cand_cnt_.ensure(static_cast<size_t>(G) + 1);
-  d_sel_cnt_.ensure(static_cast<size_t>(G) + 1);
-  const size_t ncand = static_cast<size_t>(h_cand_off_[static_cast<size_t>(G)]);
+  d_real_.ensure(R + 1);
+  d_cand_off_.ensure(R + 1);
+  d_sel_off_.ensure(R + 1);
+  d_mat_off_.ensure(R + 1);
+  d_cand_cnt_.ensure(R + 1);
+  d_sel_cnt_.ensure(R + 1);
+  const size_t ncand = static_cast<size_t>(h_cand_off_[R]);
   d_cand_.ensure(ncand + 1);
   d_res_.ensure(ncand + 1);
-  const size_t nsel = static_cast<size_t>(h_sel_off_[static_cast<size_t>(G)]);
+  const size_t nsel = static_cast<size_t>(h_sel_off_[R]);
   d_sel_keep_.ensure(nsel + 1);
   d_sel_rem_.ensure(nsel + 1);
   d_sel_gain_.ensure(nsel + 1);
-  d_sel_ok_.ensure(nsel + 1);
   d_mat_.ensure(static_cast<size_t>(max_mat) + 256);
-  if (G > 0) {
-    CheckCuda(cudaMemcpyAsync(d_cand_off_.p, h_cand_off_.data(), sizeof(long long) * static_cast<size_t>(G + 1),
+  if (R > 0) {
+    CheckCuda(cudaMemcpyAsync(d_real_.p, h_real_.data(), sizeof(int) * R, cudaMemcpyHostToDevice, stream_),
+              "h2d real");
+    CheckCuda(cudaMemcpyAsync(d_cand_off_.p, h_cand_off_.data(), sizeof(long long) * (R + 1),
                               cudaMemcpyHostToDevice, stream_), "h2d cand_off");
-    CheckCuda(cudaMemcpyAsync(d_sel_off_.p, h_sel_off_.data(), sizeof(long long) * static_cast<size_t>(G + 1),
+    CheckCuda(cudaMemcpyAsync(d_sel_off_.p, h_sel_off_.data(), sizeof(long long) * (R + 1),
                               cudaMemcpyHostToDevice, stream_), "h2d sel_off");
-    CheckCuda(cudaMemcpyAsync(d_mat_off_.p, h_mat_off_.data(), sizeof(long long) * static_cast<size_t>(G + 1),
+    CheckCuda(cudaMemcpyAsync(d_mat_off_.p, h_mat_off_.data(), sizeof(long long) * (R + 1),
                               cudaMemcpyHostToDevice, stream_), "h2d mat_off");
   }
 }
@@ -1115,17 +1155,16 @@ QuotientView Engine::View() {
   return Q;
 }
 
-void Engine::LaunchCommit(int64_t g0, int nbg, bool check_gain) {
+void Engine::LaunchCommit(int rg0, int nrg, int64_t max_pairs, bool verify) {
   CommitParams C;
   C.Q = View();
-  C.g0 = static_cast<int>(g0);
+  C.rg0 = rg0;
+  C.nrg = nrg;
   C.sel_off = d_sel_off_.p;
   C.sel_keep = d_sel_keep_.p;
   C.sel_rem = d_sel_rem_.p;
   C.sel_gain = d_sel_gain_.p;
   C.sel_cnt = d_sel_cnt_.p;
-  C.sel_ok = d_sel_ok_.p;
-  C.check_gain = check_gain ? 1 : 0;
   C.head = d_head_.p;
   C.next = d_next_.p;
   C.tail = d_tail_.p;
@@ -1135,38 +1174,31 @@ void Engine::LaunchCommit(int64_t g0, int nbg, bool check_gain) {
   C.seq = d_seq_.p;
   C.claim = d_claim_.p;
   C.block_stamp = block_stamp_;
-  C.acc_keep = d_acc_keep_.p;
-  C.acc_rem = d_acc_rem_.p;
-  C.aff = d_aff_.p;
+  C.pool_top = d_pool_top_.p;
+  C.pool_cap = pool_cap_;
+  C.scratch = d_scratch_.p;
+  C.scratch_cap = d_scratch_.n;
   C.ctl = d_ctl_.p;
   C.stats = d_stats_.p;
   C.err = d_err_.p;
-  ValidateKernel<<<nbg, 256, 0, stream_>>>(C);
-  ApplyKernel<<<nbg, 256, 0, stream_>>>(C);
-  RowsParams R;
-  R.Q = View();
-  R.stamp = d_stamp_.p;
-  R.partner = d_partner_.p;
-  R.block_stamp = block_stamp_;
-  R.acc_keep = d_acc_keep_.p;
-  R.acc_rem = d_acc_rem_.p;
-  R.aff = d_aff_.p;
-  R.ctl = d_ctl_.p;
-  R.pool_top = d_pool_top_.p;
-  R.pool_cap = pool_cap_;
-  R.scratch = d_scratch_.p;
-  R.scratch_cap = d_scratch_.n;
-  R.stats = d_stats_.p;
-  R.err = d_err_.p;
+  if (verify) {
+    const int vb = static_cast<int>(std::min<int64_t>((max_pairs + 7) / 8 + 1, 152 * 8));
+    ++launches_;
+    VerifyKernel<<<vb, 256, 0, stream_>>>(C);
+  }
+  const int grid = static_cast<int>(std::min<int64_t>(std::max<int64_t>(max_pairs, 1), kRowsGrid));
   BeginTimed(kTimeUpdate);
-  RowsKernel<<<kRowsGrid, kRowsThreads, sizeof(RowsSmem), stream_>>>(R);
+  ++launches_;
+  CommitKernel<<<grid, kRowsThreads, sizeof(RowsSmem), stream_>>>(C);
   EndTimed(kTimeUpdate);
 }
 
-void Engine::RunBlock(int64_t g0, int64_t g1, int64_t max_cap, double threshold) {
+void Engine::RunBlock(int rg0, int rg1, double threshold) {
   ++block_stamp_;
   ++hstats_.blocks;
-  const int nbg = static_cast<int>(g1 - g0);
+  const int nrg = rg1 - rg0;
+  const long long slots = h_cand_off_[static_cast<size_t>(rg1)] - h_cand_off_[static_cast<size_t>(rg0)];
+  const long long sel_slots = h_sel_off_[static_cast<size_t>(rg1)] - h_sel_off_[static_cast<size_t>(rg0)];
   CheckCuda(cudaMemsetAsync(d_ctl_.p, 0, sizeof(BlockCtl), stream_), "memset ctl");
   PrepareParams PP;
   PP.Q = View();
@@ -1175,7 +1207,8 @@ void Engine::RunBlock(int64_t g0, int64_t g1, int64_t max_cap, double threshold)
   PP.glen = d_glen_.p;
   PP.group_of = d_group_of_.p;
   PP.idx_in_group = d_idx_in_group_.p;
-  PP.g0 = static_cast<int>(g0);
+  PP.real = d_real_.p;
+  PP.rg0 = rg0;
   PP.cand_off = d_cand_off_.p;
   PP.cand = d_cand_.p;
   PP.cand_cnt = d_cand_cnt_.p;
@@ -1188,29 +1221,33 @@ void Engine::RunBlock(int64_t g0, int64_t g1, int64_t max_cap, double threshold)
   PP.stats = d_stats_.p;
   PP.err = d_err_.p;
   BeginTimed(kTimePrepare);
-  PrepareKernel<<<nbg, kPrepThreads, sizeof(PrepSmem), stream_>>>(PP);
+  ++launches_;
+  PrepareKernel<<<nrg, kPrepThreads, sizeof(PrepSmem), stream_>>>(PP);
   EndTimed(kTimePrepare);
-  if (max_cap <= 0) return;
   ScoreParams SP;
   SP.Q = View();
   SP.order = d_order_.p;
   SP.gstart = d_gstart_.p;
-  SP.g0 = static_cast<int>(g0);
+  SP.real = d_real_.p;
+  SP.rg0 = rg0;
+  SP.nrg = nrg;
   SP.cand_off = d_cand_off_.p;
   SP.cand = d_cand_.p;
   SP.cand_cnt = d_cand_cnt_.p;
   SP.res = d_res_.p;
   SP.stats = d_stats_.p;
   SP.err = d_err_.p;
-  const dim3 sgrid(static_cast<unsigned>(nbg), static_cast<unsigned>((max_cap + kPairsPerScoreCta - 1) / kPairsPerScoreCta));
+  const int sgrid = static_cast<int>(std::min<long long>((slots + 7) / 8, 152 * 16));
   BeginTimed(kTimeScore);
+  ++launches_;
   ScoreKernel<<<sgrid, kScoreThreads, 0, stream_>>>(SP);
   EndTimed(kTimeScore);
   SelectParams LP;
   LP.order = d_order_.p;
   LP.gstart = d_gstart_.p;
   LP.glen = d_glen_.p;
-  LP.g0 = static_cast<int>(g0);
+  LP.real = d_real_.p;
+  LP.rg0 = rg0;
   LP.cand_off = d_cand_off_.p;
   LP.cand = d_cand_.p;
   LP.cand_cnt = d_cand_cnt_.p;
@@ -1220,6 +1257,11 @@ void Engine::RunBlock(int64_t g0, int64_t g1, int64_t max_cap, double threshold)
   LP.sel_rem = d_sel_rem_.p;
   LP.sel_gain = d_sel_gain_.p;
   LP.sel_cnt = d_sel_cnt_.p;
+  LP.qlen = d_qlen_.p;
+  LP.stamp = d_stamp_.p;
+  LP.partner = d_partner_.p;
+  LP.seq = d_seq_.p;
+  LP.block_stamp = block_stamp_;
   LP.threshold = threshold;
   LP.use_threshold = cfg_.ea_use_threshold ? 1 : 0;
   LP.scratch = d_scratch_.p;
@@ -1227,8 +1269,9 @@ void Engine::RunBlock(int64_t g0, int64_t g1, int64_t max_cap, double threshold)
   LP.ctl = d_ctl_.p;
   LP.stats = d_stats_.p;
   LP.err = d_err_.p;
-  SelectKernel<<<nbg, kSelectThreads, 8 * kSelectSmemKeys, stream_>>>(LP);
-  LaunchCommit(g0, nbg, true);
+  ++launches_;
+  SelectKernel<<<nrg, kSelectThreads, 8 * kSelectSmemKeys, stream_>>>(LP);
+  LaunchCommit(rg0, nrg, sel_slots, cfg_.verify_cuda_gain);
 }
 
 void Engine::Merge(int iter, int total_iterations) {
@@ -1238,18 +1281,12 @@ void Engine::Merge(int iter, int total_iterations) {
   const double threshold = 1.0 / static_cast<double>(iter + 1);
   EnsurePoolRoom();
   PrepareIterationBuffers();
-  const int64_t G = n_groups_;
-  const int64_t bs = cfg_.group_batch_size;
-  const long long k = cfg_.top_k > 0 ? cfg_.top_k : 1;
-  for (int64_t b0 = 0; b0 < G; b0 += bs) {
-    const int64_t b1 = std::min(G, b0 + bs);
-    int64_t max_cap = 0;
-    for (int64_t gi = b0; gi < b1; ++gi) {
-      const long long g = h_glen_[static_cast<size_t>(gi)];
-      if (g >= 2) max_cap = std::max<int64_t>(max_cap, std::min(g * (g - 1) / 2, g * k));
-    }
-    RunBlock(b0, b1, max_cap, threshold);
+  for (size_t b = 0; b + 1 < h_block_rg_.size(); ++b) {
+    const int rg0 = h_block_rg_[b];
+    const int rg1 = h_block_rg_[b + 1];
+    if (rg1 > rg0) RunBlock(rg0, rg1, threshold);
   }
+  ++launches_;
   RelabelKernel<<<(n_ + 255) / 256, 256, 0, stream_>>>(d_label_.p, d_fwd_.p, n_);
   n_groups_ = -1;  // the groups are consumed
   CheckCuda(cudaStreamSynchronize(stream_), "merge sync");
@@ -1274,6 +1311,7 @@ void Engine::ScorePairs(const int32_t* rep_a, const int32_t* rep_b, int64_t coun
   CheckCuda(cudaMemcpyAsync(db.p, rep_b, sizeof(int) * static_cast<size_t>(count), cudaMemcpyHostToDevice, stream_),
             "h2d pairs");
   const int blocks = static_cast<int>(std::min<int64_t>((count + 7) / 8, 152 * 16));
+  ++launches_;
   ScorePairsKernel<<<blocks, 256, 0, stream_>>>(View(), da.p, db.p, count, dr.p, d_err_.p);
   std::vector<longlong2> h(static_cast<size_t>(count));
   CheckCuda(cudaMemcpyAsync(h.data(), dr.p, sizeof(longlong2) * static_cast<size_t>(count), cudaMemcpyDeviceToHost,
@@ -1297,6 +1335,7 @@ int64_t Engine::PrepareGroup(const int32_t* q, int g, int32_t* a_idx, int32_t* b
       throw std::out_of_range("quotient supernode is out of range");
     }
   }
+  if (g < 2) return 0;
   // One explicit group; the Divide output is overwritten.
   n_groups_ = 1;
   h_glen_.assign(1, g);
@@ -1307,7 +1346,7 @@ int64_t Engine::PrepareGroup(const int32_t* q, int g, int32_t* a_idx, int32_t* b
   CheckCuda(cudaMemcpyAsync(d_glen_.p, &g, sizeof(int), cudaMemcpyHostToDevice, stream_), "h2d glen");
   std::vector<int> idx(static_cast<size_t>(g));
   for (int i = 0; i < g; ++i) idx[static_cast<size_t>(i)] = i;
-  // group_of / idx_in_group for the members: everything else must not match
+  // group_of / idx_in_group for the members; every other rep must not match
   // group 0, so the array is first filled with -1.
   CheckCuda(cudaMemsetAsync(d_group_of_.p, 0xff, sizeof(int) * static_cast<size_t>(n_), stream_), "memset");
   DevBuf<int> dq, di;
@@ -1317,6 +1356,7 @@ int64_t Engine::PrepareGroup(const int32_t* q, int g, int32_t* a_idx, int32_t* b
             "h2d");
   CheckCuda(cudaMemcpyAsync(di.p, idx.data(), sizeof(int) * static_cast<size_t>(g), cudaMemcpyHostToDevice, stream_),
             "h2d");
+  ++launches_;
   ScatterGroupKernel<<<(g + 255) / 256, 256, 0, stream_>>>(dq.p, di.p, g, d_group_of_.p, d_idx_in_group_.p);
   PrepareIterationBuffers();
   CheckCuda(cudaMemsetAsync(d_ctl_.p, 0, sizeof(BlockCtl), stream_), "memset ctl");
@@ -1327,7 +1367,8 @@ int64_t Engine::PrepareGroup(const int32_t* q, int g, int32_t* a_idx, int32_t* b
   PP.glen = d_glen_.p;
   PP.group_of = d_group_of_.p;
   PP.idx_in_group = d_idx_in_group_.p;
-  PP.g0 = 0;
+  PP.real = d_real_.p;
+  PP.rg0 = 0;
   PP.cand_off = d_cand_off_.p;
   PP.cand = d_cand_.p;
   PP.cand_cnt = d_cand_cnt_.p;
@@ -1339,6 +1380,7 @@ int64_t Engine::PrepareGroup(const int32_t* q, int g, int32_t* a_idx, int32_t* b
   PP.top_k = cfg_.top_k;
   PP.stats = d_stats_.p;
   PP.err = d_err_.p;
+  ++launches_;
   PrepareKernel<<<1, kPrepThreads, sizeof(PrepSmem), stream_>>>(PP);
   int cnt = 0;
   CheckCuda(cudaMemcpyAsync(&cnt, d_cand_cnt_.p, sizeof(int), cudaMemcpyDeviceToHost, stream_), "d2h");
@@ -1369,28 +1411,38 @@ void Engine::MergePairs(const int32_t* keep, const int32_t* remove, int64_t coun
     seen[static_cast<size_t>(k)] = 1;
     seen[static_cast<size_t>(r)] = 1;
   }
+  std::vector<int> hs(static_cast<size_t>(n_));
+  CheckCuda(cudaMemcpy(hs.data(), d_qsize_.p, sizeof(int) * static_cast<size_t>(n_), cudaMemcpyDeviceToHost), "d2h");
+  for (int64_t i = 0; i < count; ++i) {
+    if (hs[static_cast<size_t>(keep[i])] <= 0 || hs[static_cast<size_t>(remove[i])] <= 0) {
+      throw std::invalid_argument("quotient supernode is inactive");
+    }
+  }
   EnsurePoolRoom();
-  // one pseudo-group holding the whole batch
-  n_groups_ = 1;
-  h_glen_.assign(1, 0);
-  PrepareIterationBuffers();
+  // the batch is one pseudo-group's selection list
+  const int cnt = static_cast<int>(count);
+  h_sel_off_.assign(2, 0);
+  h_sel_off_[1] = count;
+  d_sel_off_.ensure(2);
+  d_sel_cnt_.ensure(1);
   d_sel_keep_.ensure(static_cast<size_t>(count));
   d_sel_rem_.ensure(static_cast<size_t>(count));
   d_sel_gain_.ensure(static_cast<size_t>(count));
-  d_sel_ok_.ensure(static_cast<size_t>(count));
-  const long long zero = 0;
-  const int cnt = static_cast<int>(count);
-  CheckCuda(cudaMemcpyAsync(d_sel_off_.p, &zero, sizeof(long long), cudaMemcpyHostToDevice, stream_), "h2d");
+  CheckCuda(cudaMemcpyAsync(d_sel_off_.p, h_sel_off_.data(), 2 * sizeof(long long), cudaMemcpyHostToDevice, stream_),
+            "h2d");
   CheckCuda(cudaMemcpyAsync(d_sel_cnt_.p, &cnt, sizeof(int), cudaMemcpyHostToDevice, stream_), "h2d");
   CheckCuda(cudaMemcpyAsync(d_sel_keep_.p, keep, sizeof(int) * static_cast<size_t>(count), cudaMemcpyHostToDevice,
                             stream_), "h2d");
   CheckCuda(cudaMemcpyAsync(d_sel_rem_.p, remove, sizeof(int) * static_cast<size_t>(count), cudaMemcpyHostToDevice,
                             stream_), "h2d");
   CheckCuda(cudaMemsetAsync(d_sel_gain_.p, 0, sizeof(long long) * static_cast<size_t>(count), stream_), "memset");
-  CheckCuda(cudaMemsetAsync(d_sel_ok_.p, 1, static_cast<size_t>(count), stream_), "memset");
   ++block_stamp_;
   CheckCuda(cudaMemsetAsync(d_ctl_.p, 0, sizeof(BlockCtl), stream_), "memset ctl");
-  LaunchCommit(0, 1, false);
+  ++launches_;
+  MarkKernel<<<(cnt + 255) / 256, 256, 0, stream_>>>(d_sel_keep_.p, d_sel_rem_.p, cnt, d_stamp_.p, d_partner_.p,
+                                                    d_seq_.p, block_stamp_);
+  LaunchCommit(0, 1, count, false);
+  ++launches_;
   RelabelKernel<<<(n_ + 255) / 256, 256, 0, stream_>>>(d_label_.p, d_fwd_.p, n_);
   n_groups_ = -1;
   CheckCuda(cudaStreamSynchronize(stream_), "merge pairs sync");

@@ -108,6 +108,7 @@ class EngineOptions:
     ea_use_threshold: bool = True
     seed: int = 1
     device: int = 0
+    verify_cuda_gain: bool = False
 
 
 class Engine:
@@ -120,6 +121,7 @@ class Engine:
         cfg.top_k, cfg.group_batch_size = o.top_k, o.group_batch_size
         cfg.divide_hash_dims, cfg.divide_max_group = o.divide_hash_dims, o.divide_max_group
         cfg.ea_use_threshold, cfg.seed, cfg.device = int(o.ea_use_threshold), o.seed, o.device
+        cfg.verify_cuda_gain = int(o.verify_cuda_gain)
         h = C.c_void_p()
         N.check(N.lib().beam_engine_create(graph.n, graph.arcs, _ptr(graph.row_ptr, C.c_int64),
                                            _ptr(graph.col_idx, C.c_int32), C.byref(cfg), C.byref(h)))
@@ -227,3 +229,19 @@ class Engine:
 
     def synchronize(self) -> None:
         N.check(N.lib().beam_engine_synchronize(self._h))
+
+    def step_timer_start(self) -> None:
+        N.check(N.lib().beam_engine_step_timer_start(self._h))
+
+    def step_timer_stop(self) -> float:
+        ms = C.c_double()
+        N.check(N.lib().beam_engine_step_timer_stop(self._h, C.byref(ms)))
+        return float(ms.value)
+
+    def flush_l2(self) -> None:
+        N.check(N.lib().beam_engine_flush_l2(self._h))
+
+    def launch_count(self) -> int:
+        out = C.c_int64()
+        N.check(N.lib().beam_engine_launch_count(self._h, C.byref(out)))
+        return int(out.value)

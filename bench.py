@@ -1,0 +1,449 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 merge loop (plain GPU path, bit-exact with the
+reference) on the R-MAT scale-19 workload.
+
+A step is one full 20-iteration run of the merge loop (Divide + Merge, the
+reference's runtime_run_ms span) over the resident graph. The quotient graph
+is reset to singletons and L2 is flushed (256 MB write) before every timed
+step; both stay outside the timed span, which is measured with CUDA events on
+the engine's stream. value = accepted merges of all ranks / slowest rank's
+time. e2e runs the public C ABI from host buffers every step (create from the
+host CSR = H2D copies, 20 iterations, partition download = D2H).
+
+--impl reference times the CPU implementation of the path (the C oracle,
+a restatement of the reference pinned to its outputs) on the host cores.
+
+Multi-GPU (torchrun): replicas only - every rank runs the same workload on
+its own GPU with no collective on the data path.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "20-iter wall s & merges/s: batched+ranker vs plain GPU at equal cost ratio"
+UNIT = "merges/s"
+ITERATIONS = 20
+WORKLOAD_DESC = {
+    "rmat19": "R-MAT scale 19, edge factor 2 (a=0.57, b=0.19, c=0.19), seed 7, deduplicated, loop-free",
+    "dcsbm_4096": "degree-corrected SBM n=4096, 32 blocks, p_in/p_out=40, power-law 2.5, mean degree 43, seed 1",
+}
+FALLBACK_HBM_GBS = 6800.0
+KERNEL_CLASSES = {"score": 1, "prepare": 2, "update": 3, "divide": 4}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ------------------------------------------------------------------ dist
+
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local_rank)
+            dist.init_process_group(backend)
+            self.pg = dist
+            self.device = torch.device("cuda", self.local_rank) if backend == "nccl" else torch.device("cpu")
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def reduce(self, value: float, op: str) -> float:
+        if not self.pg:
+            return value
+        import torch
+        t = torch.tensor([value], dtype=torch.float64, device=self.device)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX if op == "max" else self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# --------------------------------------------------------------- clocks
+
+
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int, log_path: Path | None):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.log_path = log_path
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+            self.thread.join(timeout=5)
+        if self.log_path and self.rows:
+            self.log_path.write_text("\n".join(",".join(r) for r in self.rows) + "\n")
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- misc
+
+
+def measured_peak() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def profiled_traffic(kernel: str) -> float | None:
+    """DRAM bytes per launch from the committed ncu summary of this kernel."""
+    for f in sorted((ROOT / "profiles").glob(f"{kernel}*.md")):
+        for line in f.read_text().splitlines():
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                try:
+                    return float(line.split(":", 1)[1].strip().split()[0])
+                except ValueError:
+                    return None
+    return None
+
+
+def golden_hash(workload: str) -> str | None:
+    g = json.loads((ROOT / "tests" / "golden" / "golden.json").read_text())
+    for c in g["cases"]:
+        if c["name"] == workload:
+            return c["metrics"]["partition_hash"]
+    return None
+
+
+# ------------------------------------------------------------ GPU arm
+
+
+def run_ours(args, dist: Dist) -> dict | None:
+    from beam_gb300 import WORKLOADS, Engine, Graph, partition_hash
+
+    spec = WORKLOADS[args.workload]
+    t0 = time.perf_counter()
+    g = Graph.generate(spec)
+    log(f"[bench] graph {args.workload}: n={g.n} m={g.edges} ({time.perf_counter() - t0:.1f}s)")
+    device = dist.local_rank
+    e = Engine(g, device=device, ea_use_threshold=True)
+
+    # warm-up
+    for _ in range(args.warmup):
+        e.reset()
+        e.run(ITERATIONS)
+    labels, _, _ = e.partition()
+    bit_exact = None
+    want = golden_hash(args.workload)
+    if want is not None:
+        bit_exact = str(partition_hash(labels)) == want
+
+    # which kernel class dominates (untimed pass per class)
+    breakdown = {}
+    for name, kind in KERNEL_CLASSES.items():
+        e.reset()
+        e.set_timed_kernel(kind)
+        e.run(ITERATIONS)
+        ms, launches = e.timed_kernel()
+        breakdown[name] = {"ms": round(ms, 3), "launches": launches}
+    e.set_timed_kernel(0)
+    dominant = args.timed_kernel or max(breakdown, key=lambda k: breakdown[k]["ms"])
+
+    # timed region
+    dist.barrier()
+    e.synchronize()
+    step_ms = []
+    merges = 0
+    kernel_ms = 0.0
+    kernel_launches = 0
+    kernel_bytes = 0
+    launches0 = e.launch_count()
+    clock_log = ROOT / "gpurun_out" / "bench_clocks.csv" if (ROOT / "gpurun_out").exists() else None
+    wall0 = time.perf_counter()
+    with ClockSampler(device, clock_log) as clocks:
+        for _ in range(args.steps):
+            e.reset()
+            e.flush_l2()
+            st0 = e.stats()
+            e.set_timed_kernel(KERNEL_CLASSES[dominant])
+            e.step_timer_start()
+            e.run(ITERATIONS)
+            step_ms.append(e.step_timer_stop())
+            ms, launches = e.timed_kernel()
+            st1 = e.stats()
+            kernel_ms += ms
+            kernel_launches += launches
+            kernel_bytes += st1[f"{dominant}_bytes"] - st0[f"{dominant}_bytes"]
+            merges += st1["accepted_merges_after_validation"] - st0["accepted_merges_after_validation"]
+    e.synchronize()
+    launches = e.launch_count() - launches0
+    dist.barrier()
+    wall_s = time.perf_counter() - wall0
+    e.set_timed_kernel(0)
+    total_ms = sum(step_ms)
+    max_ms = dist.reduce(total_ms, "max")
+    all_merges = dist.reduce(float(merges), "sum")
+    value = all_merges / (max_ms / 1000.0)
+    ms_per_step = max_ms / args.steps
+    e.reset()
+    e.run(ITERATIONS)
+    _, head, nxt = e.partition()
+    plain_ratio = g.encode(head, nxt)["cost_ratio_mags_compatible"]
+    e.close()
+
+    # batched form: the same algorithm with one block per iteration
+    batched = None
+    if not args.no_batched:
+        eb = Engine(g, device=device, ea_use_threshold=True, group_batch_size=1 << 30)
+        eb.run(ITERATIONS)
+        bms, bmerges = [], 0
+        for _ in range(max(1, args.steps)):
+            eb.reset()
+            eb.flush_l2()
+            st0 = eb.stats()
+            eb.step_timer_start()
+            eb.run(ITERATIONS)
+            bms.append(eb.step_timer_stop())
+            bmerges += eb.stats()["accepted_merges_after_validation"] - st0["accepted_merges_after_validation"]
+        _, bhead, bnxt = eb.partition()
+        bratio = g.encode(bhead, bnxt)["cost_ratio_mags_compatible"]
+        eb.close()
+        batched = {"wall_s_20iter": round(sum(bms) / len(bms) / 1000.0, 4),
+                   "merges_per_s": round(bmerges / (sum(bms) / 1000.0), 1),
+                   "speedup_vs_plain": round(ms_per_step / (sum(bms) / len(bms)), 3),
+                   "cost_ratio_mags_compatible": round(bratio, 6),
+                   "plain_cost_ratio_mags_compatible": round(plain_ratio, 6),
+                   "cost_ratio_delta_abs": round(bratio - plain_ratio, 6),
+                   "group_batch_size": "all groups of an iteration (one block)"}
+
+    # e2e through the C ABI from host buffers
+    e2e_ms = []
+    e2e_merges = 0
+    for i in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        with Engine(g, device=device, ea_use_threshold=True) as ee:
+            ee.run(ITERATIONS)
+            ee.partition()
+            m = ee.stats()["accepted_merges_after_validation"]
+        if i >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t) * 1000.0)
+            e2e_merges += m
+    e2e_max = dist.reduce(sum(e2e_ms), "max")
+    e2e_all = dist.reduce(float(e2e_merges), "sum")
+
+    peak, peak_kind = measured_peak()
+    achieved = kernel_bytes / (kernel_ms / 1000.0) / 1e9 if kernel_ms > 0 else 0.0
+    traffic = profiled_traffic(dominant)
+    result = {
+        "metric": METRIC,
+        "value": round(value, 1),
+        "unit": UNIT,
+        "n_gpus": dist.world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_per_step, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int64",
+        "data": "synthetic (seeded generator)",
+        "config": {
+            "workload": f"{args.workload}: {WORKLOAD_DESC.get(args.workload, spec)}; n={g.n}, m={g.edges}",
+            "path": "plain GPU, 64-group blocks, bit-exact with the reference",
+            "flags": "batch-ea-blocked, mags-compatible, persistent, incremental, legacy index, certification off, "
+                     "g0, top-k 16, group-batch 64, reciprocal threshold, 20 iterations, seed 1",
+            "wall_s_20iter": round(ms_per_step / 1000.0, 4),
+            "merges_per_step": merges // max(1, args.steps),
+            "l2": "flushed by a 256 MB write before every timed step (outside the timed span)",
+            "parallelism": f"replicas x{dist.world}",
+            "bit_exact_vs_reference": bit_exact,
+        },
+        "e2e": {
+            "value": round(e2e_all / (e2e_max / 1000.0), 1) if e2e_max > 0 else None,
+            "unit": UNIT,
+            "h2d_bytes_per_step": 8 * (g.n + 1) + 4 * g.arcs,
+            "d2h_bytes_per_step": 12 * g.n,
+            "ms_per_step": round(e2e_max / max(1, args.steps), 3),
+        },
+        "gpu_launches": launches,
+        "roofline": {
+            "kernel": dominant,
+            "bound": "hbm",
+            "achieved": round(achieved, 2),
+            "peak": peak,
+            "unit": "GB/s",
+            "frac": round(achieved / peak, 5) if peak else None,
+            "peak_source": peak_kind,
+            "traffic": traffic,
+            "algorithmic_bytes_per_launch": round(kernel_bytes / max(1, kernel_launches), 1),
+            "avg_launch_us": round(1000.0 * kernel_ms / max(1, kernel_launches), 3),
+            "launches": kernel_launches,
+        },
+        "breakdown_ms_per_run": breakdown,
+        "batched": batched,
+        "clocks": clocks.summary(),
+        "wall_s_timed_region": round(wall_s, 3),
+    }
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(g, args)
+    return result
+
+
+# ------------------------------------------------------------ CPU side
+
+
+def cpu_baseline(g, args) -> dict:
+    """The oracle (C restatement of the reference path, OpenMP) on the host
+    cores: one full 20-iteration run of the same workload."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from oracle import Oracle
+
+    threads = os.cpu_count() or 1
+    o = Oracle.from_graph(g, ea_use_threshold=True, threads=threads)
+    t = time.perf_counter()
+    o.run(ITERATIONS)
+    secs = time.perf_counter() - t
+    merges = o.stats()["accepted_merges_after_validation"]
+    o.close()
+    return {"value": round(merges / secs, 1), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"one full {ITERATIONS}-iteration run of {args.workload} ({merges} merges, {secs:.2f} s)"}
+
+
+def run_reference(args, dist: Dist) -> dict | None:
+    if dist.rank != 0:
+        return None
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from oracle import Oracle
+
+    from beam_gb300 import WORKLOADS, Graph
+
+    g = Graph.generate(WORKLOADS[args.workload])
+    threads = os.cpu_count() or 1
+    times, merges = [], 0
+    for i in range(args.warmup + args.steps):
+        o = Oracle.from_graph(g, ea_use_threshold=True, threads=threads)
+        t = time.perf_counter()
+        o.run(ITERATIONS)
+        dt = time.perf_counter() - t
+        m = o.stats()["accepted_merges_after_validation"]
+        o.close()
+        if i >= args.warmup:
+            times.append(dt)
+            merges += m
+    value = merges / sum(times)
+    return {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1000.0 * sum(times) / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic (seeded generator)",
+        "impl": "reference",
+        "config": {"workload": f"{args.workload}: {WORKLOAD_DESC.get(args.workload, '')}; n={g.n}, m={g.edges}",
+                   "path": "CPU restatement of the reference path (C + OpenMP), pinned bit-exact to its outputs",
+                   "wall_s_20iter": round(sum(times) / args.steps, 4)},
+        "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"one full {ITERATIONS}-iteration run per step"},
+        "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def profile_run(args) -> None:
+    """One 20-iteration run of the workload (the unit ncu captures)."""
+    from beam_gb300 import WORKLOADS, Engine, Graph
+
+    g = Graph.generate(WORKLOADS[args.workload])
+    batch = (1 << 30) if args.batched else 64
+    with Engine(g, ea_use_threshold=True, group_batch_size=batch) as e:
+        t = time.perf_counter()
+        e.run(ITERATIONS)
+        e.synchronize()
+        st = e.stats()
+        log(f"[profile-run] {args.workload} batch={batch}: {time.perf_counter() - t:.3f} s, "
+            f"{st['accepted_merges_after_validation']} merges, {e.launch_count()} launches")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--profile-run", action="store_true", help="one run only, for ncu")
+    ap.add_argument("--batched", action="store_true", help="with --profile-run: one block per iteration")
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="rmat19")
+    ap.add_argument("--timed-kernel", choices=list(KERNEL_CLASSES), default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    args = ap.parse_args()
+    if args.profile_run:
+        profile_run(args)
+        return
+    if args.warmup < 3:
+        args.warmup = 3
+    dist = Dist()
+    try:
+        result = run_reference(args, dist) if args.impl == "reference" else run_ours(args, dist)
+        if result is not None and dist.rank == 0:
+            print(json.dumps(result), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

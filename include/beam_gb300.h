@@ -90,6 +90,8 @@ typedef struct {
   int32_t ea_use_threshold;  /* --ea-use-threshold (reciprocal policy) */
   int32_t device;            /* CUDA device ordinal */
   uint64_t seed;             /* --seed [1] */
+  int32_t verify_cuda_gain;  /* --verify-cuda-gain: re-score and check every commit */
+  int32_t reserved0;
 } beam_engine_config;
 
 /* Counters with the reference's metric names (include/sweg.hpp:221-386). */
@@ -147,6 +149,13 @@ int beam_engine_quotient_nnz(beam_engine* e, int64_t* nnz);
 int beam_engine_set_timed_kernel(beam_engine* e, int32_t which);
 int beam_engine_timed_kernel(beam_engine* e, double* ms, int64_t* launches);
 int beam_engine_synchronize(beam_engine* e);
+/* CUDA events on the engine stream around a span of work (benchmarking). */
+int beam_engine_step_timer_start(beam_engine* e);
+int beam_engine_step_timer_stop(beam_engine* e, double* ms);
+/* Overwrites a 256 MB device buffer so the next step starts with a cold L2. */
+int beam_engine_flush_l2(beam_engine* e);
+/* Kernels of this library launched by the engine since creation. */
+int beam_engine_launch_count(beam_engine* e, int64_t* launches);
 const char* beam_engine_last_error(void);
 
 /* ------------------------------------------------------- summary output */
