@@ -7,7 +7,8 @@
 // divide_max_group. The same order is produced breadth-first: every
 // unfinished segment (a run longer than divide_max_group) is already sorted by
 // rep (it is a run of equal hashes of the previous depth, tie-broken by rep),
-// so one stable segmented sort by the next hash per depth yields
+// so one stable sort by (segment, next hash) per depth - two stable LSD radix
+// passes over the unfinished items, by hash then by segment index - yields
 // (hash, rep) order inside each segment; equal-hash boundaries become new
 // segment heads. After divide_hash_dims depths the remaining long segments are
 // stably sorted by FallbackRank and cut into divide_max_group chunks. Groups
@@ -18,8 +19,8 @@
 // a supernode still in an unfinished segment, warp-aggregated atomicMin per
 // supernode, plus one self term per node.
 
+#include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
-#include <cub/device/device_segmented_sort.cuh>
 
 #include <algorithm>
 #include <numeric>
@@ -142,6 +143,27 @@ __global__ void GatherKeysKernel(const int* __restrict__ order, const int* __res
   }
 }
 
+__global__ void IotaKernel(int* __restrict__ out, int items) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < items) out[k] = k;
+}
+
+__global__ void SegKeyKernel(const int* __restrict__ item_seg, const int* __restrict__ perm, int items,
+                             int* __restrict__ segkey) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < items) segkey[j] = item_seg[perm[j]];
+}
+
+__global__ void GatherSortedKernel(const int* __restrict__ perm, int items, const unsigned long long* __restrict__ keys,
+                                   const int* __restrict__ vals, unsigned long long* __restrict__ keys_out,
+                                   int* __restrict__ vals_out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < items) {
+    keys_out[j] = keys[perm[j]];
+    vals_out[j] = vals[perm[j]];
+  }
+}
+
 __global__ void ScatterSortedKernel(const int* __restrict__ pos_map, const int* __restrict__ item_seg,
                                     const int* __restrict__ ubeg, int items,
                                     const unsigned long long* __restrict__ keys, const int* __restrict__ vals,
@@ -168,7 +190,13 @@ __global__ void GroupInfoKernel(const int* __restrict__ order, const int* __rest
   const int rep = order[p];
   group_of[rep] = s;
   idx_in_group[rep] = p - seg_start[s];
-  if (p == seg_start[s]) atomicMax(&stats[kStDivideMaxGroup], static_cast<unsigned long long>(seg_len[s]));
+  // largest group: warp maximum first, one atomic per warp
+  unsigned v = p == seg_start[s] ? static_cast<unsigned>(seg_len[s]) : 0u;
+  const unsigned active = __activemask();
+  v = __reduce_max_sync(active, v);
+  if ((threadIdx.x & 31) == __ffs(active) - 1 && v > 0) {
+    atomicMax(&stats[kStDivideMaxGroup], static_cast<unsigned long long>(v));
+  }
 }
 
 inline int Blocks(long long items, int threads) {
@@ -280,14 +308,33 @@ void Engine::Divide(int iter) {
       ++launches_;
       GatherKeysKernel<<<Blocks(items, T), T, 0, s>>>(d_order_.p, d_pos_map_.p, items, d_hash_.p, fallback ? 1 : 0,
                                                       cfg_.seed, iter, d_keys_.p, d_vals_.p);
+      // (segment, key) order, stable on the rep order inside each segment:
+      // a stable LSD radix sort by key, then a stable one by segment index.
+      ++launches_;
+      IotaKernel<<<Blocks(items, T), T, 0, s>>>(d_perm_.p, items);
       size_t bytes = 0;
-      CheckCuda(cub::DeviceSegmentedSort::StableSortPairs(nullptr, bytes, d_keys_.p, d_keys_alt_.p, d_vals_.p,
-                                                          d_vals_alt_.p, items, nu, ubeg, uend, s),
-                "cub segmented sort size");
+      CheckCuda(cub::DeviceRadixSort::SortPairs(nullptr, bytes, d_keys_.p, d_keys_alt_.p, d_perm_.p, d_perm_alt_.p,
+                                                items, 0, 64, s), "cub radix sort size");
       d_cub_tmp_.ensure(bytes);
-      CheckCuda(cub::DeviceSegmentedSort::StableSortPairs(d_cub_tmp_.p, bytes, d_keys_.p, d_keys_alt_.p, d_vals_.p,
-                                                          d_vals_alt_.p, items, nu, ubeg, uend, s),
-                "cub segmented sort");
+      CheckCuda(cub::DeviceRadixSort::SortPairs(d_cub_tmp_.p, bytes, d_keys_.p, d_keys_alt_.p, d_perm_.p,
+                                                d_perm_alt_.p, items, 0, 64, s), "cub radix sort");
+      int* perm = d_perm_alt_.p;
+      if (nu > 1) {
+        int bits = 1;
+        while ((1 << bits) < nu) ++bits;
+        ++launches_;
+        SegKeyKernel<<<Blocks(items, T), T, 0, s>>>(item_seg, d_perm_alt_.p, items, d_segkey_.p);
+        bytes = 0;
+        CheckCuda(cub::DeviceRadixSort::SortPairs(nullptr, bytes, d_segkey_.p, d_segkey_alt_.p, d_perm_alt_.p,
+                                                  d_perm_.p, items, 0, bits, s), "cub radix sort size");
+        d_cub_tmp_.ensure(bytes);
+        CheckCuda(cub::DeviceRadixSort::SortPairs(d_cub_tmp_.p, bytes, d_segkey_.p, d_segkey_alt_.p,
+                                                  d_perm_alt_.p, d_perm_.p, items, 0, bits, s), "cub radix sort");
+        perm = d_perm_.p;
+      }
+      ++launches_;
+      GatherSortedKernel<<<Blocks(items, T), T, 0, s>>>(perm, items, d_keys_.p, d_vals_.p, d_keys_alt_.p,
+                                                        d_vals_alt_.p);
       ++launches_;
       ScatterSortedKernel<<<Blocks(items, T), T, 0, s>>>(d_pos_map_.p, item_seg, ubeg, items, d_keys_alt_.p,
                                                          d_vals_alt_.p, fallback ? 1 : 0, cfg_.divide_max_group,

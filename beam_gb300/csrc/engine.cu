@@ -157,9 +157,9 @@ Engine::Engine(int n, int64_t arcs, const int64_t* row_ptr, const int32_t* col_i
   d_qsize_.ensure(un);
   d_qint_.ensure(un);
   for (DevBuf<int>* b : {&d_label_, &d_head_, &d_next_, &d_tail_, &d_fwd_, &d_stamp_, &d_partner_, &d_claim_, &d_seq_,
-                         &d_order_, &d_order_alt_, &d_head_flag_, &d_vals_, &d_vals_alt_, &d_need_, &d_seg_beg_,
+                         &d_order_, &d_head_flag_, &d_vals_, &d_vals_alt_, &d_need_, &d_seg_beg_,
                          &d_seg_end_, &d_pos_map_, &d_gstart_, &d_glen_, &d_group_of_, &d_idx_in_group_,
-                         &d_acc_keep_, &d_acc_rem_, &d_aff_}) {
+                         &d_perm_, &d_perm_alt_, &d_segkey_, &d_segkey_alt_}) {
     b->ensure(un + 1);
   }
   d_hash_.ensure(un + 1);
@@ -192,9 +192,10 @@ Engine::~Engine() {
   d_qsize_.release();
   d_qint_.release();
   for (DevBuf<int>* b : {&d_label_, &d_head_, &d_next_, &d_tail_, &d_fwd_, &d_stamp_, &d_partner_, &d_claim_, &d_seq_,
-                         &d_order_, &d_order_alt_, &d_head_flag_, &d_vals_, &d_vals_alt_, &d_need_, &d_seg_beg_,
+                         &d_order_, &d_head_flag_, &d_vals_, &d_vals_alt_, &d_need_, &d_seg_beg_,
                          &d_seg_end_, &d_pos_map_, &d_gstart_, &d_glen_, &d_group_of_, &d_idx_in_group_,
-                         &d_acc_keep_, &d_acc_rem_, &d_aff_, &d_counts_, &d_cand_cnt_, &d_sel_keep_, &d_sel_rem_,
+                         &d_perm_, &d_perm_alt_, &d_segkey_, &d_segkey_alt_, &d_counts_, &d_cand_cnt_,
+                         &d_sel_keep_, &d_sel_rem_, &d_real_,
                          &d_sel_cnt_}) {
     b->release();
   }
@@ -208,7 +209,6 @@ Engine::~Engine() {
   d_cand_.release();
   d_res_.release();
   d_sel_gain_.release();
-  d_sel_ok_.release();
   d_mat_.release();
   d_scratch_.release();
   d_ctl_.release();

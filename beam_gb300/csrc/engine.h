@@ -174,10 +174,11 @@ class Engine {
   DevBuf<int> d_stamp_, d_partner_, d_claim_, d_seq_;
 
   // divide
-  DevBuf<int> d_order_, d_order_alt_, d_head_flag_;
+  DevBuf<int> d_order_, d_head_flag_;
   DevBuf<unsigned long long> d_hash_, d_keys_, d_keys_alt_;
   DevBuf<int> d_vals_, d_vals_alt_;
   DevBuf<int> d_need_, d_seg_beg_, d_seg_end_, d_pos_map_;
+  DevBuf<int> d_perm_, d_perm_alt_, d_segkey_, d_segkey_alt_;
   DevBuf<int> d_gstart_, d_glen_, d_group_of_, d_idx_in_group_;
   DevBuf<int> d_counts_;
   DevBuf<unsigned char> d_cub_tmp_;
@@ -190,11 +191,9 @@ class Engine {
   DevBuf<int> d_cand_cnt_;
   DevBuf<int> d_sel_keep_, d_sel_rem_;
   DevBuf<long long> d_sel_gain_;
-  DevBuf<unsigned char> d_sel_ok_;
   DevBuf<int> d_sel_cnt_;
   DevBuf<unsigned char> d_mat_;
   DevBuf<unsigned char> d_scratch_;
-  DevBuf<int> d_acc_keep_, d_acc_rem_, d_aff_;
   DevBuf<BlockCtl> d_ctl_;
   DevBuf<unsigned long long> d_stats_;
   DevBuf<DevError> d_err_;

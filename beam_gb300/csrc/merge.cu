@@ -28,7 +28,8 @@
 namespace beam {
 namespace {
 
-constexpr int kPrepThreads = 256;
+constexpr int kPrepThreads = 512;
+constexpr int kLaneTopK = 32;        // per-lane candidate lists for top_k up to this
 constexpr int kSmemEntries = 2048;   // bucket entries held in shared memory
 constexpr int kSmemHeads = 4096;     // bucket hash heads in shared memory
 constexpr int kScoreThreads = 256;
@@ -352,6 +353,13 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
   examined = WarpSum(static_cast<long long>(examined));
   if (lane == 0 && examined) atomicAdd(&S.examined, examined);
   __syncthreads();
+  // mirror the upper triangle so every member's partners are one contiguous row
+  for (long long idx = tid; idx < gg; idx += kPrepThreads) {
+    const int i = static_cast<int>(idx / g);
+    const int j = static_cast<int>(idx - static_cast<long long>(i) * g);
+    if (j < i) pmat[idx] = pmat[static_cast<long long>(j) * g + i];
+  }
+  __syncthreads();
   // per member: candidates with positive proxy, ratio, top-k
   int top_k = P.top_k < g - 1 ? P.top_k : g - 1;
   if (top_k < 1) top_k = 1;
@@ -359,14 +367,11 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
     int cnt = 0;
     double* rrow = rmat + static_cast<long long>(i) * g;
     int* crow = cmat + static_cast<long long>(i) * g;
+    const long long* prow = pmat + static_cast<long long>(i) * g;
+#pragma unroll 4
     for (int base = 0; base < g; base += 32) {
       const int j = base + lane;
-      long long pg = 0;
-      if (j < g && j != i) {
-        const int a = i < j ? i : j;
-        const int b = i < j ? j : i;
-        pg = pmat[static_cast<long long>(a) * g + b];
-      }
+      const long long pg = (j < g && j != i) ? prow[j] : 0;
       const bool pred = pg > 0;
       const unsigned ball = __ballot_sync(0xffffffffu, pred);
       if (pred) {
@@ -388,6 +393,57 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
         const int a = i < j ? i : j;
         const int b = i < j ? j : i;
         fmat[static_cast<long long>(a) * g + b] = 1;
+      }
+    } else if (top_k <= kLaneTopK) {
+      // each lane keeps its best top_k candidates sorted, then the warp merges
+      // the 32 lists head by head (candidates are distinct, so no key ties)
+      RankKey lst[kLaneTopK];
+      int nl = 0;
+      for (int c = lane; c < cnt; c += 32) {
+        RankKey k;
+        k.j = crow[c];
+        k.ratio = rrow[c];
+        k.pg = prow[k.j];
+        const int qj = S.q[k.j];
+        k.lo = qi < qj ? qi : qj;
+        k.hi = qi < qj ? qj : qi;
+        if (nl == top_k && !Better(k, lst[nl - 1])) continue;
+        int pos = nl < top_k ? nl : top_k - 1;
+        while (pos > 0 && Better(k, lst[pos - 1])) {
+          lst[pos] = lst[pos - 1];
+          --pos;
+        }
+        lst[pos] = k;
+        if (nl < top_k) ++nl;
+      }
+      int head = 0;
+      for (int r = 0; r < top_k; ++r) {
+        RankKey best;
+        bool have = head < nl;
+        if (have) best = lst[head];
+        int src = lane;
+        for (int o = 16; o > 0; o >>= 1) {
+          RankKey other;
+          other.ratio = __shfl_xor_sync(0xffffffffu, best.ratio, o);
+          other.pg = __shfl_xor_sync(0xffffffffu, best.pg, o);
+          other.lo = __shfl_xor_sync(0xffffffffu, best.lo, o);
+          other.hi = __shfl_xor_sync(0xffffffffu, best.hi, o);
+          other.j = __shfl_xor_sync(0xffffffffu, best.j, o);
+          const int osrc = __shfl_xor_sync(0xffffffffu, src, o);
+          const int ohave = __shfl_xor_sync(0xffffffffu, have ? 1 : 0, o);
+          if (ohave && (!have || Better(other, best))) {
+            best = other;
+            have = true;
+            src = osrc;
+          }
+        }
+        if (!have) break;
+        if (src == lane) ++head;
+        if (lane == 0) {
+          const int a = i < best.j ? i : best.j;
+          const int b = i < best.j ? best.j : i;
+          fmat[static_cast<long long>(a) * g + b] = 1;
+        }
       }
     } else {
       RankKey prev;
