@@ -112,6 +112,8 @@ SIGNATURES = {
     "beam_engine_flush_l2": (C.c_int, [vp]),
     "beam_engine_launch_count": (C.c_int, [vp, P_i64]),
     "beam_engine_last_error": (C.c_char_p, []),
+    "beam_prepare_flat_noalloc": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, i32, i64, i32, vp, vp, i64, vp, vp]),
+    "beam_prepare_flat_noalloc_last_error": (C.c_char_p, []),
     "beam_encode": (C.c_int, [i32, i64, P_i64, P_i32, P_i32, P_i32, C.c_char_p, C.POINTER(Encoding)]),
     "beam_exact_partition_cost": (C.c_int, [i32, P_i64, P_i32, P_i32, P_i64]),
     "beam_partition_hash": (u64, [i32, P_i32]),

@@ -158,6 +158,38 @@ int beam_engine_flush_l2(beam_engine* e);
 int beam_engine_launch_count(beam_engine* e, int64_t* launches);
 const char* beam_engine_last_error(void);
 
+/* ------------------------------------------- no-allocation prepare step */
+
+/* EA-proxy candidate pairs of ONE group, for callers that cannot allocate
+ * device memory (a host that forbids cudaMalloc, a stream that must not see
+ * an allocation's implicit synchronisation, an embedder with a fixed memory
+ * budget). No counterpart in the reference: it is this library's own
+ * allocation-free form of the prepare step.
+ *
+ * Every pointer is DEVICE memory owned by the caller. Inputs follow the
+ * reference's flat per-group CSR (Sweg::FlatAggCSR): member i has reps
+ * row_rep_ids[i], size row_sizes[i], internal edge count row_internal[i] and
+ * row entries neighbors / weights / neighbor_sizes [offsets[i], offsets[i+1]);
+ * offsets has rows + 1 entries and offsets[rows] == num_entries. Output: the
+ * candidate pairs (a_idx < b_idx, ascending) in out_a_idx / out_b_idx and
+ * their number in *out_count; out_capacity must be at least
+ * min(rows*(rows-1)/2, rows*top_k). stream is a cudaStream_t (NULL = legacy
+ * default stream); the call waits for its kernel before returning.
+ *
+ * Limits: rows <= 256, num_entries <= 65536, top_k <= 32; larger requests
+ * fail with a message and launch nothing. The scratch is one static device
+ * array of about 3 MB, resident on every GPU that loads the library until the
+ * process exits, shared by all calls: its contents stay from the last call
+ * (the kernel clears what must start at zero) and calls that overlap on the
+ * GPU race. The first call on each device looks up the array's device
+ * address; make that first call before any stream capture. */
+int beam_prepare_flat_noalloc(const int32_t* offsets, const int32_t* row_rep_ids, const int32_t* neighbors,
+                              const int64_t* weights, const int64_t* neighbor_sizes, const int64_t* row_sizes,
+                              const int64_t* row_internal, int32_t rows, int64_t num_entries, int32_t top_k,
+                              int32_t* out_a_idx, int32_t* out_b_idx, int64_t out_capacity, int32_t* out_count,
+                              void* stream);
+const char* beam_prepare_flat_noalloc_last_error(void);
+
 /* ------------------------------------------------------- summary output */
 
 typedef struct {
