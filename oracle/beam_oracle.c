@@ -655,7 +655,7 @@ static void split_group(beam_oracle* o, int32_t l, int32_t r, int32_t depth, int
   }
   const int32_t dim = o->dim_order[depth];
   hrep* tmp = (hrep*)xmalloc(sizeof(hrep) * (size_t)size);
-#pragma omp parallel for schedule(dynamic, 256) if (size > 4096)
+#pragma omp parallel for schedule(dynamic, 256) if (size > 4096) num_threads(o->nthreads)
   for (int32_t k = l; k < r; ++k) {
     tmp[k - l].h = supernode_minhash(o, o->reps[k], dim, iter);
     tmp[k - l].rep = o->reps[k];
@@ -934,7 +934,8 @@ static int score_and_filter(beam_oracle* o, prepared* pr, double threshold) {
   o->st.exact_gain_input_nnz += input_nnz;
   int failed = 0;
   uint64_t raw_a = 0, raw_b = 0, uni = 0, ovl = 0;
-#pragma omp parallel for schedule(dynamic, 64) reduction(+ : raw_a, raw_b, uni, ovl) reduction(| : failed)
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : raw_a, raw_b, uni, ovl) reduction(| : failed) \
+    num_threads(o->nthreads)
   for (int64_t k = 0; k < pr->nc; ++k) {
     gain_work wk = {0, 0, 0, 0};
     if (exact_gain(o, pr->q[pr->c[k].a], pr->q[pr->c[k].b], &pr->c[k].gain, &pr->c[k].before, &wk) != 0) {
@@ -1073,7 +1074,7 @@ int beam_oracle_merge(beam_oracle* o, int iter, int total_iterations) {
     }
     const double t0 = now_ms();
     int failed = 0;
-#pragma omp parallel for schedule(dynamic, 1) if (nw > 1) reduction(| : failed)
+#pragma omp parallel for schedule(dynamic, 1) if (nw > 1) reduction(| : failed) num_threads(o->nthreads)
     for (int32_t wi = 0; wi < nw; ++wi) {
       const int32_t gi = items[wi];
       if (prepare_group(o, &o->ws[omp_get_thread_num()], o->reps + o->gstart[gi], o->glen[gi], &prep[wi]) != 0) {
