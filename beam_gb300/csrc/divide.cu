@@ -183,6 +183,7 @@ __global__ void ScatterSortedKernel(const int* __restrict__ pos_map, const int* 
 __global__ void GroupInfoKernel(const int* __restrict__ order, const int* __restrict__ incl,
                                 const int* __restrict__ seg_start, const int* __restrict__ seg_len, int count,
                                 int* __restrict__ group_of, int* __restrict__ idx_in_group,
+                                const int* __restrict__ qlen, unsigned* __restrict__ gent,
                                 unsigned long long* __restrict__ stats) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= count) return;
@@ -190,6 +191,9 @@ __global__ void GroupInfoKernel(const int* __restrict__ order, const int* __rest
   const int rep = order[p];
   group_of[rep] = s;
   idx_in_group[rep] = p - seg_start[s];
+  // row entries per group (clamped per member), used to route groups to a prepare kernel
+  const int len = qlen[rep];
+  atomicAdd(&gent[s], static_cast<unsigned>(len < (1 << 20) ? len : (1 << 20)));
   // largest group: warp maximum first, one atomic per warp
   unsigned v = p == seg_start[s] ? static_cast<unsigned>(seg_len[s]) : 0u;
   const unsigned active = __activemask();
@@ -350,9 +354,11 @@ void Engine::Divide(int iter) {
     ++launches_;
     SegLenKernel<<<Blocks(segs, T), T, 0, s>>>(seg_start, segs, count, cfg_.divide_max_group, seg_len, unf_flag,
                                                unf_len);
+    d_gent_.ensure(static_cast<size_t>(segs) + 1);
+    CheckCuda(cudaMemsetAsync(d_gent_.p, 0, sizeof(unsigned) * static_cast<size_t>(segs), s), "memset gent");
     ++launches_;
     GroupInfoKernel<<<Blocks(count, T), T, 0, s>>>(d_order_.p, scan, seg_start, seg_len, count, d_group_of_.p,
-                                                   d_idx_in_group_.p, d_stats_.p);
+                                                   d_idx_in_group_.p, d_qlen_.p, d_gent_.p, d_stats_.p);
     CheckCuda(cudaMemcpyAsync(d_gstart_.p, seg_start, sizeof(int) * static_cast<size_t>(segs),
                               cudaMemcpyDeviceToDevice, s), "copy gstart");
     CheckCuda(cudaMemcpyAsync(d_glen_.p, seg_len, sizeof(int) * static_cast<size_t>(segs),
@@ -360,9 +366,12 @@ void Engine::Divide(int iter) {
   }
   n_groups_ = segs;
   h_glen_.resize(static_cast<size_t>(segs));
+  h_gent_.resize(static_cast<size_t>(segs));
   if (segs > 0) {
     CheckCuda(cudaMemcpyAsync(h_glen_.data(), d_glen_.p, sizeof(int) * static_cast<size_t>(segs),
                               cudaMemcpyDeviceToHost, s), "d2h glen");
+    CheckCuda(cudaMemcpyAsync(h_gent_.data(), d_gent_.p, sizeof(unsigned) * static_cast<size_t>(segs),
+                              cudaMemcpyDeviceToHost, s), "d2h gent");
   }
   CheckCuda(cudaStreamSynchronize(s), "divide sync");
   hstats_.groups_last = static_cast<uint64_t>(segs);

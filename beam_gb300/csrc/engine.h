@@ -38,6 +38,10 @@ template <typename T>
 struct DevBuf {
   T* p = nullptr;
   size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
   void ensure(size_t count) {
     if (count <= n) return;
     release();
@@ -56,6 +60,10 @@ template <typename T>
 struct PinnedBuf {
   T* p = nullptr;
   size_t n = 0;
+  PinnedBuf() = default;
+  PinnedBuf(const PinnedBuf&) = delete;
+  PinnedBuf& operator=(const PinnedBuf&) = delete;
+  ~PinnedBuf() { release(); }
   void ensure(size_t count) {
     if (count <= n) return;
     release();
@@ -140,7 +148,8 @@ class Engine {
   void InitQuotient();
   void EnsurePoolRoom();
   void CompactPool();
-  void RunBlock(int rg0, int rg1, double threshold);
+  void RunBlock(size_t block, double threshold);
+  void LaunchPrepare(int s0, int s1, int b0, int b1);
   void PrepareIterationBuffers();
   void BeginTimed(int which);
   void EndTimed(int which);
@@ -198,8 +207,15 @@ class Engine {
   DevBuf<unsigned long long> d_stats_;
   DevBuf<DevError> d_err_;
   std::vector<int> h_glen_;
+  std::vector<unsigned> h_gent_;  // per group: row entries of its members at Divide time
+  DevBuf<unsigned> d_gent_;
   std::vector<int> h_real_;      // Divide ids of the groups with >= 2 members
   std::vector<int> h_block_rg_;  // per 64-group block: first real-group position
+  std::vector<int> h_small_, h_big_;              // real-group positions by prepare kernel
+  std::vector<int> h_block_small_, h_block_big_;  // per block: first entry in those lists
+  DevBuf<int> d_small_, d_big_;
+  std::vector<long long> h_big_moff_;  // member-count prefix over h_big_
+  DevBuf<long long> d_big_moff_;
   DevBuf<int> d_real_;
   std::vector<long long> h_cand_off_, h_sel_off_, h_mat_off_;
   PinnedBuf<long long> h_pin_;

@@ -33,7 +33,6 @@ constexpr int kLaneTopK = 32;        // per-lane candidate lists for top_k up to
 constexpr int kSmemEntries = 2048;   // bucket entries held in shared memory
 constexpr int kSmemHeads = 4096;     // bucket hash heads in shared memory
 constexpr int kScoreThreads = 256;
-constexpr int kPairsPerScoreCta = 64;
 constexpr int kSelectThreads = 512;
 constexpr int kSelectSmemKeys = 8192;
 constexpr int kRowsThreads = 256;
@@ -148,7 +147,10 @@ struct PrepareParams {
   const int* group_of;
   const int* idx_in_group;
   const int* real;
-  int rg0;
+  const int* list;  // real-group positions handled by this launch
+  int list0;
+  int nlist;
+  const long long* moff;  // member-count prefix over the big-group list
   const long long* cand_off;
   int2* cand;
   int* cand_cnt;
@@ -161,6 +163,10 @@ struct PrepareParams {
   unsigned long long* stats;
   DevError* err;
 };
+
+// Byte offset of the int64 old-cost array after a group's g*g tables
+// (8 + 8 + 4 + 1 bytes per member pair), rounded up to 8-byte alignment.
+__host__ __device__ __forceinline__ long long OldCostOffset(long long gg) { return (21 * gg + 7) & ~7ll; }
 
 struct RankKey {
   double ratio;
@@ -207,7 +213,7 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
   const int lane = tid & 31;
   const int warp = tid >> 5;
   const int nwarps = kPrepThreads / 32;
-  const int ri = P.rg0 + blockIdx.x;
+  const int ri = P.list[P.list0 + blockIdx.x];
   const int gid = P.real[ri];
   const int g = P.glen[gid];
   if (g < 2) {
@@ -277,12 +283,11 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
     hmask = H - 1;
   }
   for (unsigned h = tid; h <= hmask; h += kPrepThreads) heads[h] = -1;
-  // per-group pair tables
+  // per-group tables: proxy P int64[g*g] | ratio double[g*g] | partner
+  // int32[g*g] | kept flag u8[g*g] | old cost int64[g]
   const long long gg = static_cast<long long>(g) * g;
   unsigned char* mat = P.mat + P.mat_off[ri];
   long long* pmat = reinterpret_cast<long long*>(mat);
-  double* rmat = reinterpret_cast<double*>(mat + 8 * gg);
-  int* cmat = reinterpret_cast<int*>(mat + 16 * gg);
   unsigned char* fmat = mat + 20 * gg;
   for (long long k = tid; k < gg; k += kPrepThreads) {
     pmat[k] = 0;
@@ -360,10 +365,49 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
     if (j < i) pmat[idx] = pmat[static_cast<long long>(j) * g + i];
   }
   __syncthreads();
+  // old costs for the member pass, counters of the group
+  long long* old_out = reinterpret_cast<long long*>(mat + OldCostOffset(gg));
+  for (int i = tid; i < g; i += kPrepThreads) old_out[i] = S.old[i];
+  if (tid == 0) {
+    atomicAdd(&P.stats[kStGroupCount], 1ull);
+    atomicMax(&P.stats[kStGroupMaxSize], static_cast<unsigned long long>(g));
+    atomicAdd(&P.stats[kStRawPairCount], static_cast<unsigned long long>(g) * (g - 1) / 2);
+    atomicAdd(&P.stats[kStProxyExamined], S.examined);
+    // algorithmic bytes: member rows (8 B/entry) + target size gathers (4 B/entry)
+    atomicAdd(&P.stats[kStPrepareBytes], 12ull * static_cast<unsigned long long>(E));
+  }
+}
+
+// Member pass of the big groups: one warp per member of every group in the
+// launch's big-group list (moff = prefix of the member counts), so a large
+// group's members are ranked by the whole GPU instead of one CTA.
+__global__ void __launch_bounds__(256) PrepareMembersKernel(PrepareParams P) {
+  const int lane = threadIdx.x & 31;
+  const long long wg = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const long long total = P.moff[P.list0 + P.nlist] - P.moff[P.list0];
+  if (wg >= total) return;
+  const long long target = P.moff[P.list0] + wg;
+  int lo = P.list0, hi = P.list0 + P.nlist;  // last entry with moff <= target
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (P.moff[mid] <= target) lo = mid; else hi = mid;
+  }
+  const int ri = P.list[lo];
+  const int i = static_cast<int>(target - P.moff[lo]);
+  const int gid = P.real[ri];
+  const int g = P.glen[gid];
+  const int* q = P.order + P.gstart[gid];
+  const long long gg = static_cast<long long>(g) * g;
+  unsigned char* mat = P.mat + P.mat_off[ri];
+  long long* pmat = reinterpret_cast<long long*>(mat);
+  double* rmat = reinterpret_cast<double*>(mat + 8 * gg);
+  int* cmat = reinterpret_cast<int*>(mat + 16 * gg);
+  unsigned char* fmat = mat + 20 * gg;
+  const long long* old = reinterpret_cast<const long long*>(mat + OldCostOffset(gg));
   // per member: candidates with positive proxy, ratio, top-k
   int top_k = P.top_k < g - 1 ? P.top_k : g - 1;
   if (top_k < 1) top_k = 1;
-  for (int i = warp; i < g; i += nwarps) {
+  {
     int cnt = 0;
     double* rrow = rmat + static_cast<long long>(i) * g;
     int* crow = cmat + static_cast<long long>(i) * g;
@@ -378,7 +422,7 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
         const int pos = cnt + __popc(ball & ((1u << lane) - 1u));
         const int a = i < j ? i : j;
         const int b = i < j ? j : i;
-        long long denom = S.old[a] + S.old[b];
+        long long denom = old[a] + old[b];
         if (denom < 1) denom = 1;
         rrow[pos] = static_cast<double>(pg) / static_cast<double>(denom);
         crow[pos] = j;
@@ -386,7 +430,7 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
       cnt += __popc(ball);
     }
     __syncwarp();
-    const int qi = S.q[i];
+    const int qi = q[i];
     if (cnt <= top_k) {
       for (int c = lane; c < cnt; c += 32) {
         const int j = crow[c];
@@ -404,7 +448,7 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
         k.j = crow[c];
         k.ratio = rrow[c];
         k.pg = prow[k.j];
-        const int qj = S.q[k.j];
+        const int qj = q[k.j];
         k.lo = qi < qj ? qi : qj;
         k.hi = qi < qj ? qj : qi;
         if (nl == top_k && !Better(k, lst[nl - 1])) continue;
@@ -458,7 +502,7 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
           const int b = i < k.j ? k.j : i;
           k.ratio = rrow[c];
           k.pg = pmat[static_cast<long long>(a) * g + b];
-          const int qj = S.q[k.j];
+          const int qj = q[k.j];
           k.lo = qi < qj ? qi : qj;
           k.hi = qi < qj ? qj : qi;
           if (have_prev && !Better(prev, k)) continue;
@@ -492,6 +536,24 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
     }
   }
   __syncthreads();
+}
+
+// Output pass of the big groups: the union of kept pairs in (a_idx, b_idx)
+// order, one CTA per group.
+__global__ void __launch_bounds__(kPrepThreads) PrepareOutputKernel(PrepareParams P) {
+  using BlockScan = cub::BlockScan<int, kPrepThreads>;
+  __shared__ typename BlockScan::TempStorage scan_tmp;
+  __shared__ int carry;
+  __shared__ int eoff[kMaxGroup + 1];
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+  const int nwarps = kPrepThreads / 32;
+  const int ri = P.list[P.list0 + blockIdx.x];
+  const int gid = P.real[ri];
+  const int g = P.glen[gid];
+  const long long gg = static_cast<long long>(g) * g;
+  const unsigned char* fmat = P.mat + P.mat_off[ri] + 20 * gg;
   // union of kept pairs in (a_idx, b_idx) order
   for (int a = warp; a < g; a += nwarps) {
     int cnt = 0;
@@ -500,18 +562,18 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
       const bool f = b < g && fmat[static_cast<long long>(a) * g + b];
       cnt += __popc(__ballot_sync(0xffffffffu, f));
     }
-    if (lane == 0) S.eoff[a] = cnt;
+    if (lane == 0) eoff[a] = cnt;
   }
   __syncthreads();
   if (tid == 0) carry = 0;
   __syncthreads();
   for (int base = 0; base < g; base += kPrepThreads) {
     const int i = base + tid;
-    const int v = i < g ? S.eoff[i] : 0;
+    const int v = i < g ? eoff[i] : 0;
     int ex = 0, agg = 0;
     BlockScan(scan_tmp).ExclusiveSum(v, ex, agg);
     __syncthreads();
-    if (i < g) S.eoff[i] = carry + ex;
+    if (i < g) eoff[i] = carry + ex;
     __syncthreads();
     if (tid == 0) carry += agg;
     __syncthreads();
@@ -519,7 +581,7 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
   const int nc = carry;
   int2* out = P.cand + P.cand_off[ri];
   for (int a = warp; a < g; a += nwarps) {
-    int pos = S.eoff[a];
+    int pos = eoff[a];
     for (int base = a + 1; base < g; base += 32) {
       const int b = base + lane;
       const bool f = b < g && fmat[static_cast<long long>(a) * g + b];
@@ -530,12 +592,266 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
   }
   if (tid == 0) {
     P.cand_cnt[ri] = nc;
+    atomicAdd(&P.stats[kStCandAfterPrune], static_cast<unsigned long long>(nc));
+  }
+}
+
+// ------------------------------------------------------------ prepare, small groups
+
+// Groups of at most kSmallGroup members (99% of the real groups on R-MAT
+// workloads): one warp per group, no block-wide barrier. The group's rows and
+// their target sizes are staged in shared memory in one coalesced pass when
+// they fit; the EA-proxy sum over targets shared by two members then equals,
+// per member pair, the sum over the intersection of their two sorted rows (a
+// row never holds its own rep, so the reference's own-rep exclusion is
+// implied), which one lane computes per pair with a two-pointer merge while
+// the other lanes do the other pairs. Groups whose rows do not fit are handled
+// warp-cooperatively from global memory. Output and counters equal those of
+// PrepareKernel.
+constexpr int kSmallGroup = 32;
+constexpr int kSmallWarps = 4;
+constexpr int kSmallPairs = kSmallGroup * (kSmallGroup - 1) / 2;
+constexpr int kSmallStage = 480;  // staged row entries per group
+
+struct SmallWarpSmem {
+  long long p[kSmallPairs];  // upper triangle, TriIndex(a, b)
+  long long old[kSmallGroup];
+  Entry ent[kSmallStage];
+  int tsz[kSmallStage];
+  int q[kSmallGroup];
+  int sz[kSmallGroup];
+  int len[kSmallGroup];
+  int start[kSmallGroup + 1];
+  unsigned fmask[kSmallGroup];
+};
+
+struct SmallSmem {
+  SmallWarpSmem w[kSmallWarps];
+};
+
+__device__ __forceinline__ int TriIndex(int a, int b, int g) { return a * (2 * g - a - 1) / 2 + (b - a - 1); }
+
+__global__ void __launch_bounds__(kSmallWarps * 32) PrepareSmallKernel(PrepareParams P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SmallWarpSmem& S = reinterpret_cast<SmallSmem*>(smem_raw)->w[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int li = blockIdx.x * kSmallWarps + (threadIdx.x >> 5);
+  if (li >= P.nlist) return;
+  const int ri = P.list[P.list0 + li];
+  const int gid = P.real[ri];
+  const int g = P.glen[gid];
+  const QuotientView& Q = P.Q;
+  const int* order = P.order + P.gstart[gid];
+  long long off = 0;
+  int len = 0;
+  if (lane < g) {
+    const int rep = order[lane];
+    S.q[lane] = rep;
+    S.sz[lane] = Q.size[rep];
+    len = Q.len[rep];
+    off = Q.off[rep];
+    S.len[lane] = len;
+    S.fmask[lane] = 0;
+  }
+  // row starts in the staging buffer
+  int incl = len;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int E = __shfl_sync(0xffffffffu, incl, 31);
+  if (lane < g) S.start[lane] = incl - len;
+  if (lane == 0) S.start[g] = E;
+  const int npairs = g * (g - 1) / 2;
+  for (int k = lane; k < npairs; k += 32) S.p[k] = 0;
+  const bool staged = E <= kSmallStage;
+  if (staged) {
+    for (int i = 0; i < g; ++i) {
+      const long long oi = __shfl_sync(0xffffffffu, off, i);
+      const int li2 = __shfl_sync(0xffffffffu, len, i);
+      const int si = __shfl_sync(0xffffffffu, incl - len, i);
+      for (int k = lane; k < li2; k += 32) {
+        const Entry e = Q.ent[oi + k];
+        S.ent[si + k] = e;
+        S.tsz[si + k] = Q.size[EntNb(e)];
+      }
+    }
+  }
+  __syncwarp();
+  unsigned long long examined = 0;
+  if (staged) {
+    // approximate old cost: one lane per member
+    if (lane < g) {
+      const int rep = S.q[lane];
+      const long long si = S.sz[lane];
+      long long old = 0;
+      for (int k = S.start[lane]; k < S.start[lane + 1]; ++k) {
+        old += EncodeCostForPair(rep, si, EntNb(S.ent[k]), S.tsz[k], EntCnt(S.ent[k]));
+      }
+      const long long internal = Q.internal[rep];
+      if (internal > 0) old += EncodeCostForPair(rep, si, rep, si, 2 * internal);
+      S.old[lane] = old;
+    }
+    // pair proxies: one lane per member pair
+    for (int pidx = lane; pidx < npairs; pidx += 32) {
+      int a = 0, rem = pidx;
+      while (rem >= g - 1 - a) {
+        rem -= g - 1 - a;
+        ++a;
+      }
+      const int b = a + 1 + rem;
+      const int qa = S.q[a], qb = S.q[b];
+      const long long sa = S.sz[a], sb = S.sz[b];
+      int ia = S.start[a];
+      const int ea_end = S.start[a + 1];
+      int ib = S.start[b];
+      const int eb_end = S.start[b + 1];
+      long long sum = 0, direct = 0;
+      while (ia < ea_end && ib < eb_end) {
+        const int ta = EntNb(S.ent[ia]);
+        const int tb = EntNb(S.ent[ib]);
+        if (ta < tb) {
+          if (ta == qb) direct = EntCnt(S.ent[ia]);
+          ++ia;
+        } else if (tb < ta) {
+          ++ib;
+        } else {
+          const long long ea = EntCnt(S.ent[ia]);
+          const long long eb = EntCnt(S.ent[ib]);
+          const long long st = S.tsz[ia];
+          const long long delta = EncodeCostForPair(qa, sa, ta, st, ea) + EncodeCostForPair(qb, sb, ta, st, eb) -
+                                  EncodeCostForPair(qa, sa + sb, ta, st, ea + eb);
+          if (delta > 0) sum += delta;
+          ++examined;
+          ++ia;
+          ++ib;
+        }
+      }
+      for (; ia < ea_end; ++ia) {
+        if (EntNb(S.ent[ia]) == qb) direct = EntCnt(S.ent[ia]);
+      }
+      S.p[pidx] = sum + direct;
+    }
+  } else {
+    // rows too long to stage: warp-cooperative passes over global memory
+    for (int i = 0; i < g; ++i) {
+      const int rep = S.q[i];
+      const long long si = S.sz[i];
+      const long long oi = __shfl_sync(0xffffffffu, off, i);
+      const int li2 = S.len[i];
+      long long old = 0;
+      for (int k = lane; k < li2; k += 32) {
+        const Entry e = Q.ent[oi + k];
+        old += EncodeCostForPair(rep, si, EntNb(e), Q.size[EntNb(e)], EntCnt(e));
+      }
+      old = WarpSum(old);
+      if (lane == 0) {
+        const long long internal = Q.internal[rep];
+        if (internal > 0) old += EncodeCostForPair(rep, si, rep, si, 2 * internal);
+        S.old[i] = old;
+      }
+    }
+    for (int a = 0; a < g; ++a) {
+      const int qa = S.q[a];
+      const long long sa = S.sz[a];
+      const Entry* ra = Q.ent + __shfl_sync(0xffffffffu, off, a);
+      const int la = S.len[a];
+      for (int b = a + 1; b < g; ++b) {
+        const int qb = S.q[b];
+        const long long sb = S.sz[b];
+        const Entry* rb = Q.ent + __shfl_sync(0xffffffffu, off, b);
+        const int lb = S.len[b];
+        const bool a_short = la <= lb;
+        const Entry* rs = a_short ? ra : rb;
+        const Entry* rl = a_short ? rb : ra;
+        const int ls = a_short ? la : lb;
+        const int ll = a_short ? lb : la;
+        long long sum = 0;
+        int shared = 0;
+        for (int k = lane; k < ls; k += 32) {
+          const Entry e = rs[k];
+          const int t = EntNb(e);
+          const long long co = RowLookup(rl, ll, t);
+          if (co == 0) continue;
+          ++shared;
+          const long long ea = a_short ? EntCnt(e) : co;
+          const long long eb = a_short ? co : EntCnt(e);
+          const long long st = Q.size[t];
+          const long long delta = EncodeCostForPair(qa, sa, t, st, ea) + EncodeCostForPair(qb, sb, t, st, eb) -
+                                  EncodeCostForPair(qa, sa + sb, t, st, ea + eb);
+          if (delta > 0) sum += delta;
+        }
+        sum = WarpSum(sum);
+        const int sh = WarpSumInt(shared);
+        if (lane == 0) {
+          examined += static_cast<unsigned long long>(sh);
+          S.p[TriIndex(a, b, g)] = sum + RowLookup(ra, la, qb);
+        }
+      }
+    }
+  }
+  __syncwarp();
+  // per member (one lane each): positive partners, ratio, top-k
+  int top_k = P.top_k < g - 1 ? P.top_k : g - 1;
+  if (top_k < 1) top_k = 1;
+  if (lane < g) {
+    const int i = lane;
+    const int qi = S.q[i];
+    RankKey lst[kLaneTopK];
+    int nl = 0;
+    for (int j = 0; j < g; ++j) {
+      if (j == i) continue;
+      const long long pg = S.p[i < j ? TriIndex(i, j, g) : TriIndex(j, i, g)];
+      if (pg <= 0) continue;
+      long long denom = S.old[i] + S.old[j];
+      if (denom < 1) denom = 1;
+      RankKey k;
+      k.j = j;
+      k.pg = pg;
+      k.ratio = static_cast<double>(pg) / static_cast<double>(denom);
+      const int qj = S.q[j];
+      k.lo = qi < qj ? qi : qj;
+      k.hi = qi < qj ? qj : qi;
+      if (nl == top_k && !Better(k, lst[nl - 1])) continue;
+      int pos = nl < top_k ? nl : top_k - 1;
+      while (pos > 0 && Better(k, lst[pos - 1])) {
+        lst[pos] = lst[pos - 1];
+        --pos;
+      }
+      lst[pos] = k;
+      if (nl < top_k) ++nl;
+    }
+    for (int r = 0; r < nl; ++r) {
+      const int j = lst[r].j;
+      atomicOr(&S.fmask[i < j ? i : j], 1u << (i < j ? j : i));
+    }
+  }
+  __syncwarp();
+  // union of kept pairs in (a_idx, b_idx) order
+  const unsigned mine = lane < g ? S.fmask[lane] : 0u;
+  const int cnt = __popc(mine);
+  int ex = cnt;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, ex, o);
+    if (lane >= o) ex += y;
+  }
+  const int total = __shfl_sync(0xffffffffu, ex, 31);
+  ex -= cnt;
+  int2* out = P.cand + P.cand_off[ri];
+  unsigned bits = mine;
+  while (bits) {
+    const int b = __ffs(bits) - 1;
+    bits &= bits - 1;
+    out[ex++] = make_int2(lane, b);
+  }
+  examined = static_cast<unsigned long long>(WarpSum(static_cast<long long>(examined)));
+  if (lane == 0) {
+    P.cand_cnt[ri] = total;
     atomicAdd(&P.stats[kStGroupCount], 1ull);
     atomicMax(&P.stats[kStGroupMaxSize], static_cast<unsigned long long>(g));
     atomicAdd(&P.stats[kStRawPairCount], static_cast<unsigned long long>(g) * (g - 1) / 2);
-    atomicAdd(&P.stats[kStCandAfterPrune], static_cast<unsigned long long>(nc));
-    atomicAdd(&P.stats[kStProxyExamined], S.examined);
-    // algorithmic bytes: member rows (8 B/entry) + target size gathers (4 B/entry)
+    atomicAdd(&P.stats[kStCandAfterPrune], static_cast<unsigned long long>(total));
+    atomicAdd(&P.stats[kStProxyExamined], examined);
     atomicAdd(&P.stats[kStPrepareBytes], 12ull * static_cast<unsigned long long>(E));
   }
 }
@@ -1131,6 +1447,8 @@ __global__ void RelabelKernel(int* __restrict__ label, const int* __restrict__ f
 void Engine::ConfigureKernels() {
   CheckCuda(cudaFuncSetAttribute(PrepareKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(sizeof(PrepSmem))), "prepare smem attribute");
+  CheckCuda(cudaFuncSetAttribute(PrepareSmallKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(sizeof(SmallSmem))), "prepare-small smem attribute");
   CheckCuda(cudaFuncSetAttribute(SelectKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  8 * kSelectSmemKeys), "select smem attribute");
   CheckCuda(cudaFuncSetAttribute(CommitKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1165,14 +1483,48 @@ void Engine::PrepareIterationBuffers() {
     h_cand_off_[ri + 1] = h_cand_off_[ri] + std::min(g * (g - 1) / 2, g * k);
     h_sel_off_[ri + 1] = h_sel_off_[ri] + g / 2;
   }
+  // groups of at most kSmallGroup members whose rows fit the staging buffer
+  // go to the warp-per-group kernel; only the others need pair tables in
+  // global memory
+  h_small_.clear();
+  h_big_.clear();
+  h_big_moff_.assign(1, 0);
+  h_block_small_.clear();
+  h_block_big_.clear();
   for (size_t b = 0; b + 1 < h_block_rg_.size(); ++b) {
+    h_block_small_.push_back(static_cast<int>(h_small_.size()));
+    h_block_big_.push_back(static_cast<int>(h_big_.size()));
     long long off = 0;
     for (int ri = h_block_rg_[b]; ri < h_block_rg_[b + 1]; ++ri) {
-      const long long g = h_glen_[static_cast<size_t>(h_real_[static_cast<size_t>(ri)])];
+      const size_t gid = static_cast<size_t>(h_real_[static_cast<size_t>(ri)]);
+      const long long g = h_glen_[gid];
+      // rows counted at Divide time; later blocks of the same iteration may
+      // see longer rows, which the warp kernel handles unstaged
+      if (g <= kSmallGroup && h_gent_[gid] <= static_cast<unsigned>(kSmallStage)) {
+        h_small_.push_back(ri);
+        continue;
+      }
+      h_big_.push_back(ri);
+      h_big_moff_.push_back(h_big_moff_.back() + g);
       h_mat_off_[static_cast<size_t>(ri)] = off;
-      off += (21 * g * g + 255) & ~255ll;
+      off += (OldCostOffset(g * g) + 8 * g + 255) & ~255ll;  // pair tables + old costs
     }
     max_mat = std::max(max_mat, off);
+  }
+  h_block_small_.push_back(static_cast<int>(h_small_.size()));
+  h_block_big_.push_back(static_cast<int>(h_big_.size()));
+  d_small_.ensure(h_small_.size() + 1);
+  d_big_.ensure(h_big_.size() + 1);
+  if (!h_small_.empty()) {
+    CheckCuda(cudaMemcpyAsync(d_small_.p, h_small_.data(), sizeof(int) * h_small_.size(), cudaMemcpyHostToDevice,
+                              stream_), "h2d small list");
+  }
+  d_big_moff_.ensure(h_big_moff_.size());
+  if (!h_big_.empty()) {
+    CheckCuda(cudaMemcpyAsync(d_big_.p, h_big_.data(), sizeof(int) * h_big_.size(), cudaMemcpyHostToDevice,
+                              stream_), "h2d big list");
+    CheckCuda(cudaMemcpyAsync(d_big_moff_.p, h_big_moff_.data(), sizeof(long long) * h_big_moff_.size(),
+                              cudaMemcpyHostToDevice, stream_), "h2d big member offsets");
   }
   d_real_.ensure(R + 1);
   d_cand_off_.ensure(R + 1);
@@ -1249,13 +1601,9 @@ void Engine::LaunchCommit(int rg0, int nrg, int64_t max_pairs, bool verify) {
   EndTimed(kTimeUpdate);
 }
 
-void Engine::RunBlock(int rg0, int rg1, double threshold) {
-  ++block_stamp_;
-  ++hstats_.blocks;
-  const int nrg = rg1 - rg0;
-  const long long slots = h_cand_off_[static_cast<size_t>(rg1)] - h_cand_off_[static_cast<size_t>(rg0)];
-  const long long sel_slots = h_sel_off_[static_cast<size_t>(rg1)] - h_sel_off_[static_cast<size_t>(rg0)];
-  CheckCuda(cudaMemsetAsync(d_ctl_.p, 0, sizeof(BlockCtl), stream_), "memset ctl");
+// EA-proxy candidates for the small-group list entries [s0, s1) (one warp
+// per group) and the big-group entries [b0, b1) (one CTA per group).
+void Engine::LaunchPrepare(int s0, int s1, int b0, int b1) {
   PrepareParams PP;
   PP.Q = View();
   PP.order = d_order_.p;
@@ -1264,7 +1612,6 @@ void Engine::RunBlock(int rg0, int rg1, double threshold) {
   PP.group_of = d_group_of_.p;
   PP.idx_in_group = d_idx_in_group_.p;
   PP.real = d_real_.p;
-  PP.rg0 = rg0;
   PP.cand_off = d_cand_off_.p;
   PP.cand = d_cand_.p;
   PP.cand_cnt = d_cand_cnt_.p;
@@ -1277,9 +1624,40 @@ void Engine::RunBlock(int rg0, int rg1, double threshold) {
   PP.stats = d_stats_.p;
   PP.err = d_err_.p;
   BeginTimed(kTimePrepare);
-  ++launches_;
-  PrepareKernel<<<nrg, kPrepThreads, sizeof(PrepSmem), stream_>>>(PP);
+  if (s1 > s0) {
+    PP.list = d_small_.p;
+    PP.list0 = s0;
+    PP.nlist = s1 - s0;
+    ++launches_;
+    PrepareSmallKernel<<<(s1 - s0 + kSmallWarps - 1) / kSmallWarps, kSmallWarps * 32, sizeof(SmallSmem), stream_>>>(
+        PP);
+  }
+  if (b1 > b0) {
+    PP.list = d_big_.p;
+    PP.list0 = b0;
+    PP.nlist = b1 - b0;
+    PP.moff = d_big_moff_.p;
+    const long long members = h_big_moff_[static_cast<size_t>(b1)] - h_big_moff_[static_cast<size_t>(b0)];
+    ++launches_;
+    PrepareKernel<<<b1 - b0, kPrepThreads, sizeof(PrepSmem), stream_>>>(PP);
+    ++launches_;
+    PrepareMembersKernel<<<static_cast<int>((members + 7) / 8), 256, 0, stream_>>>(PP);
+    ++launches_;
+    PrepareOutputKernel<<<b1 - b0, kPrepThreads, 0, stream_>>>(PP);
+  }
   EndTimed(kTimePrepare);
+}
+
+void Engine::RunBlock(size_t b, double threshold) {
+  ++block_stamp_;
+  ++hstats_.blocks;
+  const int rg0 = h_block_rg_[b];
+  const int rg1 = h_block_rg_[b + 1];
+  const int nrg = rg1 - rg0;
+  const long long slots = h_cand_off_[static_cast<size_t>(rg1)] - h_cand_off_[static_cast<size_t>(rg0)];
+  const long long sel_slots = h_sel_off_[static_cast<size_t>(rg1)] - h_sel_off_[static_cast<size_t>(rg0)];
+  CheckCuda(cudaMemsetAsync(d_ctl_.p, 0, sizeof(BlockCtl), stream_), "memset ctl");
+  LaunchPrepare(h_block_small_[b], h_block_small_[b + 1], h_block_big_[b], h_block_big_[b + 1]);
   ScoreParams SP;
   SP.Q = View();
   SP.order = d_order_.p;
@@ -1338,9 +1716,7 @@ void Engine::Merge(int iter, int total_iterations) {
   EnsurePoolRoom();
   PrepareIterationBuffers();
   for (size_t b = 0; b + 1 < h_block_rg_.size(); ++b) {
-    const int rg0 = h_block_rg_[b];
-    const int rg1 = h_block_rg_[b + 1];
-    if (rg1 > rg0) RunBlock(rg0, rg1, threshold);
+    if (h_block_rg_[b + 1] > h_block_rg_[b]) RunBlock(b, threshold);
   }
   ++launches_;
   RelabelKernel<<<(n_ + 255) / 256, 256, 0, stream_>>>(d_label_.p, d_fwd_.p, n_);
@@ -1395,6 +1771,7 @@ int64_t Engine::PrepareGroup(const int32_t* q, int g, int32_t* a_idx, int32_t* b
   // One explicit group; the Divide output is overwritten.
   n_groups_ = 1;
   h_glen_.assign(1, g);
+  h_gent_.assign(1, 0u);
   const int zero = 0;
   CheckCuda(cudaMemcpyAsync(d_order_.p, hq.data(), sizeof(int) * static_cast<size_t>(g), cudaMemcpyHostToDevice,
                             stream_), "h2d group");
@@ -1416,28 +1793,7 @@ int64_t Engine::PrepareGroup(const int32_t* q, int g, int32_t* a_idx, int32_t* b
   ScatterGroupKernel<<<(g + 255) / 256, 256, 0, stream_>>>(dq.p, di.p, g, d_group_of_.p, d_idx_in_group_.p);
   PrepareIterationBuffers();
   CheckCuda(cudaMemsetAsync(d_ctl_.p, 0, sizeof(BlockCtl), stream_), "memset ctl");
-  PrepareParams PP;
-  PP.Q = View();
-  PP.order = d_order_.p;
-  PP.gstart = d_gstart_.p;
-  PP.glen = d_glen_.p;
-  PP.group_of = d_group_of_.p;
-  PP.idx_in_group = d_idx_in_group_.p;
-  PP.real = d_real_.p;
-  PP.rg0 = 0;
-  PP.cand_off = d_cand_off_.p;
-  PP.cand = d_cand_.p;
-  PP.cand_cnt = d_cand_cnt_.p;
-  PP.mat_off = d_mat_off_.p;
-  PP.mat = d_mat_.p;
-  PP.scratch = d_scratch_.p;
-  PP.scratch_cap = d_scratch_.n;
-  PP.ctl = d_ctl_.p;
-  PP.top_k = cfg_.top_k;
-  PP.stats = d_stats_.p;
-  PP.err = d_err_.p;
-  ++launches_;
-  PrepareKernel<<<1, kPrepThreads, sizeof(PrepSmem), stream_>>>(PP);
+  LaunchPrepare(0, static_cast<int>(h_small_.size()), 0, static_cast<int>(h_big_.size()));
   int cnt = 0;
   CheckCuda(cudaMemcpyAsync(&cnt, d_cand_cnt_.p, sizeof(int), cudaMemcpyDeviceToHost, stream_), "d2h");
   CheckCuda(cudaStreamSynchronize(stream_), "prepare sync");

@@ -415,7 +415,9 @@ def profile_run(args) -> None:
         e.synchronize()
         st = e.stats()
         log(f"[profile-run] {args.workload} batch={batch}: {time.perf_counter() - t:.3f} s, "
-            f"{st['accepted_merges_after_validation']} merges, {e.launch_count()} launches")
+            f"{st['accepted_merges_after_validation']} merges, {e.launch_count()} launches, "
+            f"divide {st['runtime_divide_ms']:.1f} ms, merge {st['runtime_merge_ms']:.1f} ms, "
+            f"blocks {st['blocks']}, compactions {st['pool_compactions']}")
 
 
 def main():
