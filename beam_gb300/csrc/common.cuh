@@ -69,6 +69,7 @@ enum ErrCode : int {
   kErrValidation = 6,       // commit-time gain differs from the scored gain
   kErrKeyRange = 7,         // gain outside the packed sort-key range
   kErrInactive = 8,         // scoring request on an inactive supernode
+  kErrSlots = 9,            // a group's row entries exceed its sort slots
 };
 
 struct DevError {

@@ -191,9 +191,9 @@ __global__ void GroupInfoKernel(const int* __restrict__ order, const int* __rest
   const int rep = order[p];
   group_of[rep] = s;
   idx_in_group[rep] = p - seg_start[s];
-  // row entries per group (clamped per member), used to route groups to a prepare kernel
-  const int len = qlen[rep];
-  atomicAdd(&gent[s], static_cast<unsigned>(len < (1 << 20) ? len : (1 << 20)));
+  // row entries per group: routing to a prepare kernel and, as an upper
+  // bound for the iteration, the deferred groups' sort slots
+  atomicAdd(&gent[s], static_cast<unsigned>(qlen[rep]));
   // largest group: warp maximum first, one atomic per warp
   unsigned v = p == seg_start[s] ? static_cast<unsigned>(seg_len[s]) : 0u;
   const unsigned active = __activemask();

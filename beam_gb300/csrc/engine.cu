@@ -254,6 +254,7 @@ void Engine::CheckError() {
     case kErrValidation: msg = "commit-time exact gain differs from the scored gain"; break;
     case kErrKeyRange: msg = "merge gain outside the selection key range"; break;
     case kErrInactive: msg = "quotient supernode is inactive or endpoints are equal"; break;
+    case kErrSlots: msg = "group row entries exceed their prepare sort slots"; break;
     default: msg = "device error"; break;
   }
   msg += " (" + std::to_string(e.a) + ", " + std::to_string(e.b) + ", " + std::to_string(e.c) + ")";

@@ -214,6 +214,10 @@ class Engine {
   std::vector<int> h_small_, h_big_;              // real-group positions by prepare kernel
   std::vector<int> h_block_small_, h_block_big_;  // per block: first entry in those lists
   DevBuf<int> d_small_, d_big_;
+  DevBuf<unsigned char> d_bigdesc_;  // per big-group entry: deferred-group descriptor
+  std::vector<long long> h_soff_;    // sort-slot prefix over h_big_ (deferred groups)
+  DevBuf<long long> d_soff_;
+  DevBuf<unsigned long long> d_skey_[2], d_sval_[2];
   std::vector<long long> h_big_moff_;  // member-count prefix over h_big_
   DevBuf<long long> d_big_moff_;
   DevBuf<int> d_real_;

@@ -20,6 +20,7 @@
 // the reference's sequential incremental updates.
 
 #include <cub/block/block_scan.cuh>
+#include <cub/device/device_radix_sort.cuh>
 
 #include <algorithm>
 
@@ -139,6 +140,41 @@ __device__ void WarpExactGain(const QuotientView& Q, int a, int b, long long* ga
 // sel_off, sel_cnt) are indexed by the group's position in the iteration's
 // list of groups with at least two members ("real" groups); real[ri] is the
 // Divide group id. A block covers the real groups [rg0, rg0 + nrg).
+// A big group whose row entries (counted at Divide time, an upper bound for
+// the rest of the iteration: rows of supernodes not yet merged only shrink)
+// exceed the shared-memory bucket table is deferred. PrepareKernel stages its
+// row offsets and member scalars in block scratch; PrepareFillKernel writes
+// one (group, target) key and one (member, count) value per row entry into
+// the group's sort slots, a radix sort brings the entries of every
+// (group, target) together, and PrepareAccumKernel accumulates the member
+// pairs of each run with contiguous reads. No group is bound to one SM.
+// Scratch layout: eoff int32[g+1] | mq int32[g] | msz int32[g].
+struct BigDesc {
+  unsigned char* base;  // nullptr: not deferred
+  int E;
+  int pad;
+};
+
+struct DeferredView {
+  int* eoff;
+  int* mq;
+  int* msz;
+};
+
+__host__ __device__ __forceinline__ unsigned long long DeferredBytes(int g) {
+  return 4ull * (3ull * static_cast<unsigned long long>(g) + 1);
+}
+
+__device__ __forceinline__ DeferredView Deferred(unsigned char* base, int g) {
+  DeferredView V;
+  V.eoff = reinterpret_cast<int*>(base);
+  V.mq = V.eoff + g + 1;
+  V.msz = V.mq + g;
+  return V;
+}
+
+constexpr unsigned long long kSlotPad = ~0ull;  // key of an unused sort slot
+
 struct PrepareParams {
   QuotientView Q;
   const int* order;
@@ -151,6 +187,14 @@ struct PrepareParams {
   int list0;
   int nlist;
   const long long* moff;  // member-count prefix over the big-group list
+  BigDesc* desc;          // per big-group list entry
+  const long long* soff;  // sort-slot prefix over the big-group list (0 slots: not deferred)
+  long long slot0;        // soff of the launch's first entry
+  unsigned long long* skey;  // unsorted keys / values of the launch's slots
+  unsigned long long* sval;
+  const unsigned long long* skey_sorted;
+  const unsigned long long* sval_sorted;
+  long long nslots;
   const long long* cand_off;
   int2* cand;
   int* cand_cnt;
@@ -216,6 +260,19 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
   const int ri = P.list[P.list0 + blockIdx.x];
   const int gid = P.real[ri];
   const int g = P.glen[gid];
+  BigDesc* desc = P.desc + P.list0 + blockIdx.x;
+  if (tid == 0) {
+    desc->base = nullptr;
+    desc->E = 0;
+  }
+  // sort slots of a deferred group start as padding, so that every exit
+  // below leaves them well-defined for the sort and the accumulate pass
+  const long long slot_beg = P.soff[P.list0 + blockIdx.x];
+  const long long slots = P.soff[P.list0 + blockIdx.x + 1] - slot_beg;
+  {
+    unsigned long long* key = P.skey + (slot_beg - P.slot0);
+    for (long long k = tid; k < slots; k += kPrepThreads) key[k] = kSlotPad;
+  }
   if (g < 2) {
     if (tid == 0) P.cand_cnt[ri] = 0;
     return;
@@ -254,41 +311,72 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
   }
   const int E = carry;
   if (tid == 0) S.eoff[g] = E;
-  // bucket table: shared memory when it fits, block scratch otherwise
+  const long long gg = static_cast<long long>(g) * g;
+  unsigned char* mat = P.mat + P.mat_off[ri];
+  long long* pmat = reinterpret_cast<long long*>(mat);
+  unsigned char* fmat = mat + 20 * gg;
+  if (slots > 0) {
+    // deferred group: row offsets and member scalars in block scratch, pair
+    // tables zeroed, unused sort slots padded; fill / sort / accumulate follow
+    if (E > slots) {
+      if (tid == 0) {
+        RaiseError(P.err, kErrSlots, gid, E, static_cast<int>(slots));
+        P.cand_cnt[ri] = 0;
+      }
+      return;
+    }
+    __shared__ unsigned char* dbase;
+    if (tid == 0) {
+      dbase = reinterpret_cast<unsigned char*>(ScratchAlloc(P.scratch, P.scratch_cap, P.ctl, DeferredBytes(g), P.err));
+    }
+    __syncthreads();
+    if (dbase == nullptr) {
+      if (tid == 0) P.cand_cnt[ri] = 0;
+      return;
+    }
+    const DeferredView V = Deferred(dbase, g);
+    long long* old_out = reinterpret_cast<long long*>(mat + OldCostOffset(gg));
+    for (int i = tid; i < g; i += kPrepThreads) {
+      V.eoff[i] = S.eoff[i];
+      V.mq[i] = S.q[i];
+      V.msz[i] = S.sz[i];
+      // the fill pass adds the row terms of the approximate old cost
+      const long long si = S.sz[i];
+      const long long internal = Q.internal[S.q[i]];
+      old_out[i] = internal > 0 ? EncodeCostForPair(S.q[i], si, S.q[i], si, 2 * internal) : 0;
+    }
+    if (tid == 0) V.eoff[g] = E;
+    for (long long k = tid; k < gg; k += kPrepThreads) {
+      pmat[k] = 0;
+      fmat[k] = 0;
+    }
+    if (tid == 0) {
+      desc->base = dbase;
+      desc->E = E;
+      atomicAdd(&P.stats[kStGroupCount], 1ull);
+      atomicMax(&P.stats[kStGroupMaxSize], static_cast<unsigned long long>(g));
+      atomicAdd(&P.stats[kStRawPairCount], static_cast<unsigned long long>(g) * (g - 1) / 2);
+      atomicAdd(&P.stats[kStPrepareBytes], 12ull * static_cast<unsigned long long>(E));
+    }
+    return;
+  }
+  if (E > kSmemEntries) {
+    if (tid == 0) {
+      RaiseError(P.err, kErrSlots, gid, E, 0);
+      P.cand_cnt[ri] = 0;
+    }
+    return;
+  }
+  // bucket table in shared memory
   int* heads = S.heads;
   int* et = S.et;
   int* ei = S.ei;
   unsigned* ee = S.ee;
   int* enx = S.enx;
-  unsigned hmask = kSmemHeads - 1;
-  __shared__ unsigned long long* big;
-  if (E > kSmemEntries) {
-    unsigned H = 64;
-    while (H < 2u * static_cast<unsigned>(E)) H <<= 1;
-    if (tid == 0) {
-      big = ScratchAlloc(P.scratch, P.scratch_cap, P.ctl,
-                         static_cast<unsigned long long>(E) * 16ull + static_cast<unsigned long long>(H) * 4ull, P.err);
-    }
-    __syncthreads();
-    if (big == nullptr) {
-      if (tid == 0) P.cand_cnt[ri] = 0;
-      return;
-    }
-    unsigned char* b = reinterpret_cast<unsigned char*>(big);
-    heads = reinterpret_cast<int*>(b);
-    et = reinterpret_cast<int*>(b + 4ull * H);
-    ei = et + E;
-    ee = reinterpret_cast<unsigned*>(ei + E);
-    enx = reinterpret_cast<int*>(ee + E);
-    hmask = H - 1;
-  }
+  const unsigned hmask = kSmemHeads - 1;
   for (unsigned h = tid; h <= hmask; h += kPrepThreads) heads[h] = -1;
   // per-group tables: proxy P int64[g*g] | ratio double[g*g] | partner
   // int32[g*g] | kept flag u8[g*g] | old cost int64[g]
-  const long long gg = static_cast<long long>(g) * g;
-  unsigned char* mat = P.mat + P.mat_off[ri];
-  long long* pmat = reinterpret_cast<long long*>(mat);
-  unsigned char* fmat = mat + 20 * gg;
   for (long long k = tid; k < gg; k += kPrepThreads) {
     pmat[k] = 0;
     fmat[k] = 0;
@@ -376,6 +464,118 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
     // algorithmic bytes: member rows (8 B/entry) + target size gathers (4 B/entry)
     atomicAdd(&P.stats[kStPrepareBytes], 12ull * static_cast<unsigned long long>(E));
   }
+}
+
+// Fill pass of the deferred groups, grid (big-group entry, slice): one
+// thread per row entry of the group (entries of one member are contiguous,
+// found by a binary search of the row offsets staged in shared memory), so a
+// hub member's long row is spread over many warps. Per entry: its sort key
+// (launch-local group index, target) and value (member, count), the entry's
+// approximate-old-cost term (summed per member by a
+// segmented warp scan, one atomic per member run), and direct in-group edges,
+// which go to both halves of the pair table (row i holds j and row j holds i
+// with the same count), so no mirror pass is needed.
+constexpr int kFillThreads = 256;
+constexpr int kAccumThreads = 256;
+
+__global__ void __launch_bounds__(kFillThreads) PrepareFillKernel(PrepareParams P) {
+  __shared__ int eoff_s[kMaxGroup + 1];
+  const BigDesc d = P.desc[P.list0 + blockIdx.x];
+  if (d.base == nullptr) return;
+  const int lane = threadIdx.x & 31;
+  const int ri = P.list[P.list0 + blockIdx.x];
+  const int gid = P.real[ri];
+  const int g = P.glen[gid];
+  const long long gg = static_cast<long long>(g) * g;
+  unsigned char* mat = P.mat + P.mat_off[ri];
+  long long* pmat = reinterpret_cast<long long*>(mat);
+  unsigned long long* old_out = reinterpret_cast<unsigned long long*>(mat + OldCostOffset(gg));
+  const DeferredView V = Deferred(d.base, g);
+  const long long slot = P.soff[P.list0 + blockIdx.x] - P.slot0;
+  const unsigned long long key_hi = static_cast<unsigned long long>(blockIdx.x) << 32;
+  for (int i = threadIdx.x; i <= g; i += kFillThreads) eoff_s[i] = V.eoff[i];
+  __syncthreads();
+  const QuotientView& Q = P.Q;
+  const int stride = gridDim.y * kFillThreads;
+  for (int base = blockIdx.y * kFillThreads; base < d.E; base += stride) {
+    const int idx = base + threadIdx.x;
+    int i = -1;
+    long long cost = 0;
+    if (idx < d.E) {
+      int lo = 0, hi = g;  // last member with eoff <= idx
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (eoff_s[mid] <= idx) lo = mid; else hi = mid;
+      }
+      i = lo;
+      const int rep = V.mq[i];
+      const Entry e = Q.ent[Q.off[rep] + (idx - eoff_s[i])];
+      const int t = EntNb(e);
+      const long long c = EntCnt(e);
+      cost = EncodeCostForPair(rep, V.msz[i], t, Q.size[t], c);
+      P.skey[slot + idx] = key_hi | static_cast<unsigned>(t);
+      P.sval[slot + idx] = static_cast<unsigned long long>(i) << 32 | static_cast<unsigned long long>(c);
+      if (P.group_of[t] == gid) pmat[static_cast<long long>(i) * g + P.idx_in_group[t]] = c;
+    }
+    // segmented inclusive scan over runs of equal member index
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long vc = __shfl_up_sync(0xffffffffu, cost, o);
+      const int vi = __shfl_up_sync(0xffffffffu, i, o);
+      if (lane >= o && vi == i) cost += vc;
+    }
+    const int next_i = __shfl_down_sync(0xffffffffu, i, 1);
+    if (i >= 0 && (lane == 31 || next_i != i) && cost != 0) {
+      atomicAdd(&old_out[i], static_cast<unsigned long long>(cost));
+    }
+  }
+}
+
+// Accumulate pass of the deferred groups over the sorted slots: the entries
+// of one (group, target) are a contiguous run; the thread at run position p
+// pairs its member with the members at positions before p in the run, so each
+// member pair sharing a target is visited once, and adds
+// proxy += max(0, old - new) to both halves of the pair table.
+__global__ void __launch_bounds__(kAccumThreads) PrepareAccumKernel(PrepareParams P) {
+  unsigned long long examined = 0;
+  const long long stride = static_cast<long long>(gridDim.x) * kAccumThreads;
+  for (long long p = static_cast<long long>(blockIdx.x) * kAccumThreads + threadIdx.x; p < P.nslots; p += stride) {
+    const unsigned long long key = P.skey_sorted[p];
+    if (key == kSlotPad) continue;
+    if (p == 0 || P.skey_sorted[p - 1] != key) continue;  // run head: no earlier entry
+    const int bl = static_cast<int>(key >> 32);
+    const int t = static_cast<int>(key & 0xffffffffu);
+    if (bl >= P.nlist) continue;
+    const BigDesc d = P.desc[P.list0 + bl];
+    const int ri = P.list[P.list0 + bl];
+    const int g = P.glen[P.real[ri]];
+    long long* pmat = reinterpret_cast<long long*>(P.mat + P.mat_off[ri]);
+    const DeferredView V = Deferred(d.base, g);
+    const unsigned long long vi = P.sval_sorted[p];
+    const int i = static_cast<int>(vi >> 32);
+    const long long c = static_cast<long long>(vi & 0xffffffffu);
+    const long long st = P.Q.size[t];
+    const long long si = V.msz[i];
+    const int qi = V.mq[i];
+    for (long long q = p - 1; q >= 0 && P.skey_sorted[q] == key; --q) {
+      const unsigned long long vj = P.sval_sorted[q];
+      const int j = static_cast<int>(vj >> 32);
+      const long long cj = static_cast<long long>(vj & 0xffffffffu);
+      const long long sj = V.msz[j];
+      const int qj = V.mq[j];
+      ++examined;
+      const long long oldc = EncodeCostForPair(qi, si, t, st, c) + EncodeCostForPair(qj, sj, t, st, cj);
+      const long long newc = EncodeCostForPair(qi, si + sj, t, st, c + cj);
+      const long long delta = oldc - newc;
+      if (delta > 0) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&pmat[static_cast<long long>(i) * g + j]),
+                  static_cast<unsigned long long>(delta));
+        atomicAdd(reinterpret_cast<unsigned long long*>(&pmat[static_cast<long long>(j) * g + i]),
+                  static_cast<unsigned long long>(delta));
+      }
+    }
+  }
+  examined = static_cast<unsigned long long>(WarpSum(static_cast<long long>(examined)));
+  if ((threadIdx.x & 31) == 0 && examined) atomicAdd(&P.stats[kStProxyExamined], examined);
 }
 
 // Member pass of the big groups: one warp per member of every group in the
@@ -1489,6 +1689,7 @@ void Engine::PrepareIterationBuffers() {
   h_small_.clear();
   h_big_.clear();
   h_big_moff_.assign(1, 0);
+  h_soff_.assign(1, 0);
   h_block_small_.clear();
   h_block_big_.clear();
   for (size_t b = 0; b + 1 < h_block_rg_.size(); ++b) {
@@ -1498,14 +1699,17 @@ void Engine::PrepareIterationBuffers() {
     for (int ri = h_block_rg_[b]; ri < h_block_rg_[b + 1]; ++ri) {
       const size_t gid = static_cast<size_t>(h_real_[static_cast<size_t>(ri)]);
       const long long g = h_glen_[gid];
-      // rows counted at Divide time; later blocks of the same iteration may
-      // see longer rows, which the warp kernel handles unstaged
+      // rows counted at Divide time (rows of supernodes not merged yet only
+      // shrink during an iteration, so the count is an upper bound)
       if (g <= kSmallGroup && h_gent_[gid] <= static_cast<unsigned>(kSmallStage)) {
         h_small_.push_back(ri);
         continue;
       }
       h_big_.push_back(ri);
       h_big_moff_.push_back(h_big_moff_.back() + g);
+      // groups beyond the shared-memory bucket table get sort slots
+      const long long e_ub = h_gent_[gid];
+      h_soff_.push_back(h_soff_.back() + (e_ub > kSmemEntries ? e_ub : 0));
       h_mat_off_[static_cast<size_t>(ri)] = off;
       off += (OldCostOffset(g * g) + 8 * g + 255) & ~255ll;  // pair tables + old costs
     }
@@ -1515,6 +1719,19 @@ void Engine::PrepareIterationBuffers() {
   h_block_big_.push_back(static_cast<int>(h_big_.size()));
   d_small_.ensure(h_small_.size() + 1);
   d_big_.ensure(h_big_.size() + 1);
+  d_bigdesc_.ensure(sizeof(BigDesc) * (h_big_.size() + 1));
+  long long max_slots = 1;
+  for (size_t b = 0; b + 1 < h_block_big_.size(); ++b) {
+    max_slots = std::max(max_slots, h_soff_[static_cast<size_t>(h_block_big_[b + 1])] -
+                                        h_soff_[static_cast<size_t>(h_block_big_[b])]);
+  }
+  for (int k = 0; k < 2; ++k) {
+    d_skey_[k].ensure(static_cast<size_t>(max_slots));
+    d_sval_[k].ensure(static_cast<size_t>(max_slots));
+  }
+  d_soff_.ensure(h_soff_.size());
+  CheckCuda(cudaMemcpyAsync(d_soff_.p, h_soff_.data(), sizeof(long long) * h_soff_.size(), cudaMemcpyHostToDevice,
+                            stream_), "h2d soff");
   if (!h_small_.empty()) {
     CheckCuda(cudaMemcpyAsync(d_small_.p, h_small_.data(), sizeof(int) * h_small_.size(), cudaMemcpyHostToDevice,
                               stream_), "h2d small list");
@@ -1638,8 +1855,38 @@ void Engine::LaunchPrepare(int s0, int s1, int b0, int b1) {
     PP.nlist = b1 - b0;
     PP.moff = d_big_moff_.p;
     const long long members = h_big_moff_[static_cast<size_t>(b1)] - h_big_moff_[static_cast<size_t>(b0)];
+    PP.desc = reinterpret_cast<BigDesc*>(d_bigdesc_.p);
+    PP.soff = d_soff_.p;
+    PP.slot0 = h_soff_[static_cast<size_t>(b0)];
+    PP.nslots = h_soff_[static_cast<size_t>(b1)] - PP.slot0;
+    PP.skey = d_skey_[0].p;
+    PP.sval = d_sval_[0].p;
+    PP.skey_sorted = d_skey_[1].p;
+    PP.sval_sorted = d_sval_[1].p;
+    // slices per deferred group: about 2048 row entries per CTA of the
+    // largest group (row totals as counted at Divide time)
+    long long max_e = 0;
+    for (int b = b0; b < b1; ++b) {
+      max_e = std::max(max_e, h_soff_[static_cast<size_t>(b) + 1] - h_soff_[static_cast<size_t>(b)]);
+    }
     ++launches_;
     PrepareKernel<<<b1 - b0, kPrepThreads, sizeof(PrepSmem), stream_>>>(PP);
+    if (PP.nslots > 0) {
+      const unsigned slices = static_cast<unsigned>(std::min(512ll, std::max(1ll, (max_e + 2047) / 2048)));
+      ++launches_;
+      PrepareFillKernel<<<dim3(b1 - b0, slices), kFillThreads, 0, stream_>>>(PP);
+      int bits = 32;
+      while ((1ll << (bits - 32)) < b1 - b0) ++bits;
+      size_t bytes = 0;
+      CheckCuda(cub::DeviceRadixSort::SortPairs(nullptr, bytes, d_skey_[0].p, d_skey_[1].p, d_sval_[0].p,
+                                                d_sval_[1].p, PP.nslots, 0, bits, stream_), "cub radix sort size");
+      d_cub_tmp_.ensure(bytes);
+      CheckCuda(cub::DeviceRadixSort::SortPairs(d_cub_tmp_.p, bytes, d_skey_[0].p, d_skey_[1].p, d_sval_[0].p,
+                                                d_sval_[1].p, PP.nslots, 0, bits, stream_), "cub radix sort");
+      const long long want = (PP.nslots + kAccumThreads - 1) / kAccumThreads;
+      ++launches_;
+      PrepareAccumKernel<<<static_cast<int>(std::min(want, 152ll * 16)), kAccumThreads, 0, stream_>>>(PP);
+    }
     ++launches_;
     PrepareMembersKernel<<<static_cast<int>((members + 7) / 8), 256, 0, stream_>>>(PP);
     ++launches_;
@@ -1771,7 +2018,16 @@ int64_t Engine::PrepareGroup(const int32_t* q, int g, int32_t* a_idx, int32_t* b
   // One explicit group; the Divide output is overwritten.
   n_groups_ = 1;
   h_glen_.assign(1, g);
-  h_gent_.assign(1, 0u);
+  // the group's row entries (routing and deferred-group sort slots)
+  {
+    std::vector<int> lens(static_cast<size_t>(n_));
+    CheckCuda(cudaMemcpyAsync(lens.data(), d_qlen_.p, sizeof(int) * static_cast<size_t>(n_), cudaMemcpyDeviceToHost,
+                              stream_), "d2h row lengths");
+    CheckCuda(cudaStreamSynchronize(stream_), "sync");
+    unsigned e = 0;
+    for (int i = 0; i < g; ++i) e += static_cast<unsigned>(lens[static_cast<size_t>(hq[static_cast<size_t>(i)])]);
+    h_gent_.assign(1, e);
+  }
   const int zero = 0;
   CheckCuda(cudaMemcpyAsync(d_order_.p, hq.data(), sizeof(int) * static_cast<size_t>(g), cudaMemcpyHostToDevice,
                             stream_), "h2d group");

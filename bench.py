@@ -1,14 +1,17 @@
 #!/usr/bin/env python
-"""Benchmark of the GB300 merge loop (plain GPU path, bit-exact with the
-reference) on the R-MAT scale-19 workload.
+"""Benchmark of the GB300 merge loop on the R-MAT scale-19 workload.
 
 A step is one full 20-iteration run of the merge loop (Divide + Merge, the
 reference's runtime_run_ms span) over the resident graph. The quotient graph
 is reset to singletons and L2 is flushed (256 MB write) before every timed
 step; both stay outside the timed span, which is measured with CUDA events on
 the engine's stream. value = accepted merges of all ranks / slowest rank's
-time. e2e runs the public C ABI from host buffers every step (create from the
-host CSR = H2D copies, 20 iterations, partition download = D2H).
+time for the headline form (--form, default batched: one block of all groups
+per iteration); the other form (plain: the reference's 64-group blocks,
+bit-exact with the reference) is timed beside it for the speed-up and the
+cost-ratio comparison. e2e runs the public C ABI from host buffers every step
+(create from the host CSR = H2D copies, 20 iterations, partition download =
+D2H).
 
 --impl reference times the CPU implementation of the path (the C oracle,
 a restatement of the reference pinned to its outputs) on the host cores.
@@ -176,121 +179,156 @@ def golden_hash(workload: str) -> str | None:
 # ------------------------------------------------------------ GPU arm
 
 
+FORMS = {
+    # one block per iteration: every group of an iteration is prepared, scored,
+    # selected and committed by one launch of each kernel
+    "batched": 1 << 30,
+    # the reference's 64-group blocks: bit-exact with the reference CPU path
+    "plain": 64,
+}
+
+
+def form_engine(g, device: int, form: str):
+    from beam_gb300 import Engine
+
+    return Engine(g, device=device, ea_use_threshold=True, group_batch_size=FORMS[form])
+
+
+def kernel_breakdown(e) -> dict:
+    """Device time per kernel class over one untimed 20-iteration run each."""
+    out = {}
+    for name, kind in KERNEL_CLASSES.items():
+        e.reset()
+        e.set_timed_kernel(kind)
+        e.run(ITERATIONS)
+        ms, launches = e.timed_kernel()
+        out[name] = {"ms": round(ms, 3), "launches": launches}
+    e.set_timed_kernel(0)
+    return out
+
+
+def timed_steps(e, steps: int, dominant: str | None) -> dict:
+    """steps x (reset, L2 flush, timed 20-iteration run); CUDA events on the
+    engine stream around each run, the dominant kernel class timed inside."""
+    step_ms, merges, kernel_ms, kernel_launches, kernel_bytes, step_launches = [], 0, 0.0, 0, 0, 0
+    for _ in range(steps):
+        e.reset()
+        e.flush_l2()
+        st0 = e.stats()
+        if dominant:
+            e.set_timed_kernel(KERNEL_CLASSES[dominant])
+        launches0 = e.launch_count()
+        e.step_timer_start()
+        e.run(ITERATIONS)
+        step_ms.append(e.step_timer_stop())
+        step_launches += e.launch_count() - launches0
+        st1 = e.stats()
+        if dominant:
+            ms, launches = e.timed_kernel()
+            kernel_ms += ms
+            kernel_launches += launches
+            kernel_bytes += st1[f"{dominant}_bytes"] - st0[f"{dominant}_bytes"]
+        merges += st1["accepted_merges_after_validation"] - st0["accepted_merges_after_validation"]
+    e.synchronize()
+    e.set_timed_kernel(0)
+    return {"step_ms": step_ms, "merges": merges, "kernel_ms": kernel_ms, "kernel_launches": kernel_launches,
+            "kernel_bytes": kernel_bytes, "launches": step_launches}
+
+
+def final_cost_ratio(e, g) -> tuple[float, str]:
+    from beam_gb300 import partition_hash
+
+    e.reset()
+    e.run(ITERATIONS)
+    labels, head, nxt = e.partition()
+    return g.encode(head, nxt)["cost_ratio_mags_compatible"], str(partition_hash(labels))
+
+
 def run_ours(args, dist: Dist) -> dict | None:
-    from beam_gb300 import WORKLOADS, Engine, Graph, partition_hash
+    from beam_gb300 import WORKLOADS, Graph
 
     spec = WORKLOADS[args.workload]
     t0 = time.perf_counter()
     g = Graph.generate(spec)
     log(f"[bench] graph {args.workload}: n={g.n} m={g.edges} ({time.perf_counter() - t0:.1f}s)")
     device = dist.local_rank
-    e = Engine(g, device=device, ea_use_threshold=True)
+    head_form = args.form
+    other_form = "plain" if head_form == "batched" else "batched"
+    want = golden_hash(args.workload)
 
-    # warm-up
+    # headline form: warm-up, kernel breakdown, timed region
+    e = form_engine(g, device, head_form)
     for _ in range(args.warmup):
         e.reset()
         e.run(ITERATIONS)
-    labels, _, _ = e.partition()
-    bit_exact = None
-    want = golden_hash(args.workload)
-    if want is not None:
-        bit_exact = str(partition_hash(labels)) == want
-
-    # which kernel class dominates (untimed pass per class)
-    breakdown = {}
-    for name, kind in KERNEL_CLASSES.items():
-        e.reset()
-        e.set_timed_kernel(kind)
-        e.run(ITERATIONS)
-        ms, launches = e.timed_kernel()
-        breakdown[name] = {"ms": round(ms, 3), "launches": launches}
-    e.set_timed_kernel(0)
+    breakdown = kernel_breakdown(e)
     dominant = args.timed_kernel or max(breakdown, key=lambda k: breakdown[k]["ms"])
-
-    # timed region
     dist.barrier()
     e.synchronize()
-    step_ms = []
-    merges = 0
-    kernel_ms = 0.0
-    kernel_launches = 0
-    kernel_bytes = 0
-    launches0 = e.launch_count()
     clock_log = ROOT / "gpurun_out" / "bench_clocks.csv" if (ROOT / "gpurun_out").exists() else None
     wall0 = time.perf_counter()
     with ClockSampler(device, clock_log) as clocks:
-        for _ in range(args.steps):
-            e.reset()
-            e.flush_l2()
-            st0 = e.stats()
-            e.set_timed_kernel(KERNEL_CLASSES[dominant])
-            e.step_timer_start()
-            e.run(ITERATIONS)
-            step_ms.append(e.step_timer_stop())
-            ms, launches = e.timed_kernel()
-            st1 = e.stats()
-            kernel_ms += ms
-            kernel_launches += launches
-            kernel_bytes += st1[f"{dominant}_bytes"] - st0[f"{dominant}_bytes"]
-            merges += st1["accepted_merges_after_validation"] - st0["accepted_merges_after_validation"]
-    e.synchronize()
-    launches = e.launch_count() - launches0
+        t = timed_steps(e, args.steps, dominant)
     dist.barrier()
     wall_s = time.perf_counter() - wall0
-    e.set_timed_kernel(0)
-    total_ms = sum(step_ms)
+    total_ms = sum(t["step_ms"])
     max_ms = dist.reduce(total_ms, "max")
-    all_merges = dist.reduce(float(merges), "sum")
+    all_merges = dist.reduce(float(t["merges"]), "sum")
     value = all_merges / (max_ms / 1000.0)
     ms_per_step = max_ms / args.steps
-    e.reset()
-    e.run(ITERATIONS)
-    _, head, nxt = e.partition()
-    plain_ratio = g.encode(head, nxt)["cost_ratio_mags_compatible"]
+    head_ratio, head_hash = final_cost_ratio(e, g)
     e.close()
+    forms = {head_form: {"wall_s_20iter": round(ms_per_step / 1000.0, 4),
+                         "merges_per_s": round(value / dist.world, 1),
+                         "merges_per_step": t["merges"] // max(1, args.steps),
+                         "cost_ratio_mags_compatible": round(head_ratio, 6),
+                         "partition_hash": head_hash,
+                         "group_batch_size": FORMS[head_form]}}
 
-    # batched form: the same algorithm with one block per iteration
-    batched = None
-    if not args.no_batched:
-        eb = Engine(g, device=device, ea_use_threshold=True, group_batch_size=1 << 30)
-        eb.run(ITERATIONS)
-        bms, bmerges = [], 0
-        for _ in range(max(1, args.steps)):
-            eb.reset()
-            eb.flush_l2()
-            st0 = eb.stats()
-            eb.step_timer_start()
-            eb.run(ITERATIONS)
-            bms.append(eb.step_timer_stop())
-            bmerges += eb.stats()["accepted_merges_after_validation"] - st0["accepted_merges_after_validation"]
-        _, bhead, bnxt = eb.partition()
-        bratio = g.encode(bhead, bnxt)["cost_ratio_mags_compatible"]
-        eb.close()
-        batched = {"wall_s_20iter": round(sum(bms) / len(bms) / 1000.0, 4),
-                   "merges_per_s": round(bmerges / (sum(bms) / 1000.0), 1),
-                   "speedup_vs_plain": round(ms_per_step / (sum(bms) / len(bms)), 3),
-                   "cost_ratio_mags_compatible": round(bratio, 6),
-                   "plain_cost_ratio_mags_compatible": round(plain_ratio, 6),
-                   "cost_ratio_delta_abs": round(bratio - plain_ratio, 6),
-                   "group_batch_size": "all groups of an iteration (one block)"}
+    # the other form, for the speed-up and the cost-ratio comparison
+    if not args.no_other_form:
+        eo = form_engine(g, device, other_form)
+        eo.reset()
+        eo.run(ITERATIONS)
+        o_steps = max(1, min(args.steps, 3))
+        to = timed_steps(eo, o_steps, None)
+        o_ms = sum(to["step_ms"]) / o_steps
+        o_ratio, o_hash = final_cost_ratio(eo, g)
+        eo.close()
+        forms[other_form] = {"wall_s_20iter": round(o_ms / 1000.0, 4),
+                             "merges_per_s": round(to["merges"] / (sum(to["step_ms"]) / 1000.0), 1),
+                             "merges_per_step": to["merges"] // o_steps,
+                             "cost_ratio_mags_compatible": round(o_ratio, 6),
+                             "partition_hash": o_hash,
+                             "group_batch_size": FORMS[other_form], "steps": o_steps}
+    if "plain" in forms:
+        forms["plain"]["bit_exact_vs_reference"] = None if want is None else forms["plain"]["partition_hash"] == want
+    comparison = None
+    if "plain" in forms and "batched" in forms:
+        comparison = {
+            "speedup_batched_vs_plain": round(forms["plain"]["wall_s_20iter"] / forms["batched"]["wall_s_20iter"], 3),
+            "cost_ratio_delta_abs": round(forms["batched"]["cost_ratio_mags_compatible"]
+                                          - forms["plain"]["cost_ratio_mags_compatible"], 6),
+        }
 
-    # e2e through the C ABI from host buffers
-    e2e_ms = []
-    e2e_merges = 0
+    # e2e through the C ABI from host buffers: create from the host CSR
+    # (H2D), 20 iterations, partition download (D2H)
+    e2e_ms, e2e_merges = [], 0
     for i in range(args.warmup + args.steps):
-        t = time.perf_counter()
-        with Engine(g, device=device, ea_use_threshold=True) as ee:
+        t1 = time.perf_counter()
+        with form_engine(g, device, head_form) as ee:
             ee.run(ITERATIONS)
             ee.partition()
             m = ee.stats()["accepted_merges_after_validation"]
         if i >= args.warmup:
-            e2e_ms.append((time.perf_counter() - t) * 1000.0)
+            e2e_ms.append((time.perf_counter() - t1) * 1000.0)
             e2e_merges += m
     e2e_max = dist.reduce(sum(e2e_ms), "max")
     e2e_all = dist.reduce(float(e2e_merges), "sum")
 
     peak, peak_kind = measured_peak()
-    achieved = kernel_bytes / (kernel_ms / 1000.0) / 1e9 if kernel_ms > 0 else 0.0
+    kernel_ms, kernel_launches = t["kernel_ms"], t["kernel_launches"]
+    achieved = t["kernel_bytes"] / (kernel_ms / 1000.0) / 1e9 if kernel_ms > 0 else 0.0
     traffic = profiled_traffic(dominant)
     result = {
         "metric": METRIC,
@@ -307,15 +345,17 @@ def run_ours(args, dist: Dist) -> dict | None:
         "data": "synthetic (seeded generator)",
         "config": {
             "workload": f"{args.workload}: {WORKLOAD_DESC.get(args.workload, spec)}; n={g.n}, m={g.edges}",
-            "path": "plain GPU, 64-group blocks, bit-exact with the reference",
+            "form": head_form,
+            "path": ("batched GPU form: one block of all groups per iteration"
+                     if head_form == "batched" else "plain GPU form: 64-group blocks, bit-exact with the reference"),
             "flags": "batch-ea-blocked, mags-compatible, persistent, incremental, legacy index, certification off, "
-                     "g0, top-k 16, group-batch 64, reciprocal threshold, 20 iterations, seed 1",
+                     "g0, top-k 16, reciprocal threshold, 20 iterations, seed 1",
             "wall_s_20iter": round(ms_per_step / 1000.0, 4),
-            "merges_per_step": merges // max(1, args.steps),
             "l2": "flushed by a 256 MB write before every timed step (outside the timed span)",
             "parallelism": f"replicas x{dist.world}",
-            "bit_exact_vs_reference": bit_exact,
         },
+        "forms": forms,
+        "comparison": comparison,
         "e2e": {
             "value": round(e2e_all / (e2e_max / 1000.0), 1) if e2e_max > 0 else None,
             "unit": UNIT,
@@ -323,7 +363,7 @@ def run_ours(args, dist: Dist) -> dict | None:
             "d2h_bytes_per_step": 12 * g.n,
             "ms_per_step": round(e2e_max / max(1, args.steps), 3),
         },
-        "gpu_launches": launches,
+        "gpu_launches": t["launches"],
         "roofline": {
             "kernel": dominant,
             "bound": "hbm",
@@ -333,12 +373,11 @@ def run_ours(args, dist: Dist) -> dict | None:
             "frac": round(achieved / peak, 5) if peak else None,
             "peak_source": peak_kind,
             "traffic": traffic,
-            "algorithmic_bytes_per_launch": round(kernel_bytes / max(1, kernel_launches), 1),
+            "algorithmic_bytes_per_launch": round(t["kernel_bytes"] / max(1, kernel_launches), 1),
             "avg_launch_us": round(1000.0 * kernel_ms / max(1, kernel_launches), 3),
             "launches": kernel_launches,
         },
         "breakdown_ms_per_run": breakdown,
-        "batched": batched,
         "clocks": clocks.summary(),
         "wall_s_timed_region": round(wall_s, 3),
     }
@@ -425,13 +464,15 @@ def main():
     ap.add_argument("--profile-run", action="store_true", help="one run only, for ncu")
     ap.add_argument("--batched", action="store_true", help="with --profile-run: one block per iteration")
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="rmat19")
     ap.add_argument("--timed-kernel", choices=list(KERNEL_CLASSES), default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--form", choices=list(FORMS), default="batched",
+                    help="form whose throughput is the headline value")
+    ap.add_argument("--no-other-form", action="store_true", help="skip timing the other form")
     args = ap.parse_args()
     if args.profile_run:
         profile_run(args)

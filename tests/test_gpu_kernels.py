@@ -164,3 +164,23 @@ def test_hub_rows_and_large_groups():
     compare_state(e, o, g.n)
     assert e.stats()["accepted_merges_after_validation"] == o.stats()["accepted_merges_after_validation"]
     e.close()
+
+
+@pytest.mark.parametrize("name", ["rmat12", "dcsbm", "chunglu_twins"])
+def test_batched_form_matches_oracle(name):
+    """The batched form (one block of all groups per iteration) is the same
+    algorithm with a larger block; the oracle with the same block size gives
+    the same partition and counters."""
+    from beam_gb300 import partition_hash
+    batch = 1 << 30
+    g, e, o = pair(SPECS[name], group_batch_size=batch)
+    e.run(20)
+    o.run(20)
+    assert partition_hash(e.partition()[0]) == o.partition_hash()
+    st, ost = e.stats(), o.stats()
+    for k in ("accepted_merges_after_validation", "merge_exact_gain_calls", "candidate_proxy_pairs_examined",
+              "update_touched_quotient_entries", "blocks"):
+        if k in ost:
+            assert st[k] == ost[k], k
+    assert 1 <= st["blocks"] <= 20
+    e.close()
