@@ -5,7 +5,7 @@ The compute path is libbeam_gb300.so (hand-written CUDA kernels + C++
 runtime); this package only binds it.
 """
 
-from .engine import Engine, EngineOptions, Graph, partition_hash
+from .engine import Engine, EngineOptions, Graph, partition_hash, ranker_grad
 
 # Seeded synthetic stand-ins for the five workloads of the benchmark plan.
 WORKLOADS = {
@@ -26,4 +26,4 @@ REFERENCE_FLAGS = [
     "--seed", "1", "--error-bound", "0.0",
 ]
 
-__all__ = ["Engine", "EngineOptions", "Graph", "partition_hash", "WORKLOADS", "REFERENCE_FLAGS"]
+__all__ = ["Engine", "EngineOptions", "Graph", "partition_hash", "ranker_grad", "WORKLOADS", "REFERENCE_FLAGS"]

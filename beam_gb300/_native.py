@@ -28,7 +28,14 @@ class EngineConfig(C.Structure):
         ("device", i32),
         ("seed", u64),
         ("verify_cuda_gain", i32),
-        ("reserved0", i32),
+        ("ranker", i32),
+        ("ranker_train_iters", i32),
+        ("ranker_recall", C.c_float),
+        ("ranker_audit", i32),
+        ("ranker_max_samples", i32),
+        ("ranker_epochs", i32),
+        ("ranker_max_steps", i32),
+        ("ranker_lr", C.c_float),
     ]
 
 
@@ -55,6 +62,16 @@ class EngineStats(C.Structure):
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class RankerInfo(C.Structure):
+    _fields_ = [(name, u64) for name in ("samples", "positives", "train_steps", "ranked", "pruned",
+                                          "audit_passing", "audit_lost")] + [
+        (name, f64) for name in ("train_ms", "first_loss", "final_loss", "cutoff", "calib_recall", "calib_prune")
+    ] + [("trained", i32), ("reserved", i32)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
 
 
 class Encoding(C.Structure):
@@ -104,6 +121,9 @@ SIGNATURES = {
     "beam_engine_export_row": (C.c_int, [vp, i32, P_i32, P_i64, i64, P_i64, P_i64, P_i64]),
     "beam_engine_get_stats": (C.c_int, [vp, C.POINTER(EngineStats)]),
     "beam_engine_quotient_nnz": (C.c_int, [vp, P_i64]),
+    "beam_engine_ranker_info": (C.c_int, [vp, C.POINTER(RankerInfo)]),
+    "beam_ranker_grad": (C.c_int, [i32, vp, vp, vp, i64, vp, vp, P_f64, vp]),
+    "beam_ranker_last_error": (C.c_char_p, []),
     "beam_engine_set_timed_kernel": (C.c_int, [vp, i32]),
     "beam_engine_timed_kernel": (C.c_int, [vp, P_f64, P_i64]),
     "beam_engine_synchronize": (C.c_int, [vp]),

@@ -55,6 +55,10 @@ enum Stat : int {
   kStPrepareBytes,            // algorithmic bytes of the prepare kernel
   kStUpdateBytes,             // algorithmic bytes of the row-update kernels
   kStDivideBytes,             // algorithmic bytes of the min-hash kernel
+  kStRkRanked,                // candidate pairs scored by the ranker
+  kStRkPruned,                // of which pruned before exact scoring
+  kStRkAuditPassing,          // audit: ranked pairs passing the threshold filter
+  kStRkAuditLost,             // audit: pruned pairs among them
   kStCount
 };
 
@@ -170,6 +174,16 @@ __device__ __forceinline__ int RowLowerBound(const Entry* row, int len, int key)
 __device__ __forceinline__ long long RowLookup(const Entry* row, int len, int key) {
   const int p = RowLowerBound(row, len, key);
   return (p < len && EntNb(row[p]) == key) ? EntCnt(row[p]) : 0;
+}
+
+// Index of the real group owning a candidate slot: last ri in [lo, hi) with
+// off[ri] <= slot.
+__device__ __forceinline__ int OwnerOfSlot(const long long* off, int lo, int hi, long long slot) {
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (off[mid] <= slot) lo = mid; else hi = mid;
+  }
+  return lo;
 }
 
 // Device view of the quotient graph.

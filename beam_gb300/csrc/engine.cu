@@ -238,6 +238,7 @@ void Engine::Reset() {
   n_groups_ = -1;
   n_active_ = n_;
   hstats_ = HostStats{};
+  RankerReset();
 }
 
 void Engine::CheckError() {
@@ -495,7 +496,14 @@ void beam_engine_default_config(beam_engine_config* cfg) {
   cfg->device = 0;
   cfg->seed = 1;
   cfg->verify_cuda_gain = 0;
-  cfg->reserved0 = 0;
+  cfg->ranker = 0;
+  cfg->ranker_train_iters = 5;
+  cfg->ranker_recall = 0.99f;
+  cfg->ranker_audit = 0;
+  cfg->ranker_max_samples = 1 << 18;
+  cfg->ranker_epochs = 4;
+  cfg->ranker_max_steps = 256;
+  cfg->ranker_lr = 3e-3f;
 }
 
 int beam_engine_create(int32_t n, int64_t arcs, const int64_t* row_ptr, const int32_t* col_idx,
@@ -513,6 +521,27 @@ int beam_engine_create(int32_t n, int64_t arcs, const int64_t* row_ptr, const in
       c.seed = cfg->seed;
       c.device = cfg->device;
       c.verify_cuda_gain = cfg->verify_cuda_gain != 0;
+      c.ranker = cfg->ranker != 0;
+      c.ranker_train_iters = cfg->ranker_train_iters;
+      c.ranker_recall = cfg->ranker_recall;
+      c.ranker_audit = cfg->ranker_audit != 0;
+      c.ranker_max_samples = cfg->ranker_max_samples;
+      c.ranker_epochs = cfg->ranker_epochs;
+      c.ranker_max_steps = cfg->ranker_max_steps;
+      c.ranker_lr = cfg->ranker_lr;
+      if (c.ranker) {
+        if (c.ranker_train_iters < 1) throw std::invalid_argument("ranker_train_iters must be >= 1");
+        if (!(c.ranker_recall > 0.0f && c.ranker_recall <= 1.0f)) {
+          throw std::invalid_argument("ranker_recall must be in (0, 1]");
+        }
+        if (c.ranker_max_samples < 1024 || c.ranker_max_samples > (1 << 24)) {
+          throw std::invalid_argument("ranker_max_samples must be in [1024, 2^24]");
+        }
+        if (c.ranker_epochs < 1 || c.ranker_max_steps < 16 || c.ranker_max_steps > 1024) {
+          throw std::invalid_argument("ranker_epochs >= 1 and ranker_max_steps in [16, 1024] required");
+        }
+        if (!(c.ranker_lr > 0.0f)) throw std::invalid_argument("ranker_lr must be positive");
+      }
     }
     auto* e = new beam_engine{new Engine(n, arcs, row_ptr, col_idx, c)};
     *out = e;
@@ -618,6 +647,29 @@ int beam_engine_get_stats(beam_engine* e, beam_engine_stats* out) {
     out->pool_compactions = h.compactions;
     out->active_supernodes = h.active_last;
     out->groups_last = h.groups_last;
+  });
+}
+
+int beam_engine_ranker_info(beam_engine* e, beam_ranker_info* out) {
+  return Guard([&] {
+    uint64_t c[beam::kStCount];
+    e->impl->DeviceStats(c, beam::kStCount);
+    const beam::RankerInfo& r = e->impl->ranker_info();
+    std::memset(out, 0, sizeof(*out));
+    out->samples = r.samples;
+    out->positives = r.positives;
+    out->train_steps = r.train_steps;
+    out->ranked = c[beam::kStRkRanked];
+    out->pruned = c[beam::kStRkPruned];
+    out->audit_passing = c[beam::kStRkAuditPassing];
+    out->audit_lost = c[beam::kStRkAuditLost];
+    out->train_ms = r.train_ms;
+    out->first_loss = r.first_loss;
+    out->final_loss = r.final_loss;
+    out->cutoff = r.cutoff;
+    out->calib_recall = r.calib_recall;
+    out->calib_prune = r.calib_prune;
+    out->trained = r.trained ? 1 : 0;
   });
 }
 

@@ -24,6 +24,21 @@ struct EngineConfig {
   int device = 0;
   // Re-score every selected pair at commit and check it (--verify-cuda-gain).
   bool verify_cuda_gain = false;
+  // Learned candidate ranker (off: the reference's method).
+  bool ranker = false;
+  int ranker_train_iters = 5;
+  float ranker_recall = 0.99f;
+  bool ranker_audit = false;
+  int ranker_max_samples = 1 << 18;
+  int ranker_epochs = 4;
+  int ranker_max_steps = 256;
+  float ranker_lr = 3e-3f;
+};
+
+struct RankerInfo {
+  uint64_t samples = 0, positives = 0, train_steps = 0;
+  double train_ms = 0, first_loss = 0, final_loss = 0, cutoff = 0, calib_recall = 0, calib_prune = 0;
+  bool trained = false;
 };
 
 // Largest group the kernels accept (bounded by the packed select keys and
@@ -123,6 +138,7 @@ class Engine {
   void DeviceStats(uint64_t* out, int count);
   int64_t QuotientNnz();
   const HostStats& host_stats() const { return hstats_; }
+  const RankerInfo& ranker_info() const { return rk_info_; }
   int64_t active_count() const { return n_active_; }
   int64_t group_count() const { return n_groups_; }
   int n() const { return n_; }
@@ -148,7 +164,15 @@ class Engine {
   void InitQuotient();
   void EnsurePoolRoom();
   void CompactPool();
-  void RunBlock(size_t block, double threshold);
+  void RunBlock(size_t block, double threshold, int iter, int total_iterations);
+  void RankerReset();
+  void RankerEnsure();
+  void RankerLog(int rg0, int nrg, long long slots, int iter, double threshold, int total_iterations);
+  void RankerRank(int rg0, int nrg, long long slots, double threshold, int iter);
+  void RankerCutoff(long long slots);
+  long long RankerExploreCap(long long slots) const;
+  void RankerTrain();
+  void RankerFinishIteration();
   void LaunchPrepare(int s0, int s1, int b0, int b1);
   void PrepareIterationBuffers();
   void BeginTimed(int which);
@@ -227,6 +251,22 @@ class Engine {
   int64_t n_active_ = 0;
   int64_t n_groups_ = 0;
   HostStats hstats_;
+
+  // learned candidate ranker
+  DevBuf<float2> d_cand_feat_;
+  DevBuf<unsigned char> d_rk_keep_;
+  DevBuf<float> d_rk_x_, d_rk_y_, d_rk_x2_, d_rk_y2_;  // training log, as appended / in (iteration, slot) order
+  DevBuf<unsigned long long> d_rk_key_[2];
+  DevBuf<int> d_rk_idx_[2];
+  DevBuf<unsigned> d_rk_count_, d_rk_ticket_, d_rk_npos_;
+  DevBuf<float> d_rk_params_, d_rk_m_, d_rk_v_, d_rk_norm_, d_rk_partial_, d_rk_loss_;
+  DevBuf<unsigned short> d_rk_wbf_;
+  DevBuf<double> d_rk_npartial_;
+  DevBuf<float> d_rk_zbuf_, d_rk_zpos_[2], d_rk_cut_;  // per-slot logits, exploration positives, cutoff
+  bool rk_trained_ = false;
+  float rk_cutoff_ = 0.0f;
+  long long rk_iter_slots_ = 0;
+  RankerInfo rk_info_;
 
   // launch accounting and step timing
   int64_t launches_ = 0;

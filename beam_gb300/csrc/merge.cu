@@ -188,6 +188,7 @@ struct PrepareParams {
   int nlist;
   const long long* moff;  // member-count prefix over the big-group list
   BigDesc* desc;          // per big-group list entry
+  float2* cand_feat;      // per candidate: proxy gain, proxy ratio (ranker features; nullptr: off)
   const long long* soff;  // sort-slot prefix over the big-group list (0 slots: not deferred)
   long long slot0;        // soff of the launch's first entry
   unsigned long long* skey;  // unsorted keys / values of the launch's slots
@@ -754,6 +755,8 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareOutputKernel(PrepareParam
   const int g = P.glen[gid];
   const long long gg = static_cast<long long>(g) * g;
   const unsigned char* fmat = P.mat + P.mat_off[ri] + 20 * gg;
+  const long long* pmat = reinterpret_cast<const long long*>(P.mat + P.mat_off[ri]);
+  const long long* old = reinterpret_cast<const long long*>(P.mat + P.mat_off[ri] + OldCostOffset(gg));
   // union of kept pairs in (a_idx, b_idx) order
   for (int a = warp; a < g; a += nwarps) {
     int cnt = 0;
@@ -786,7 +789,17 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareOutputKernel(PrepareParam
       const int b = base + lane;
       const bool f = b < g && fmat[static_cast<long long>(a) * g + b];
       const unsigned ball = __ballot_sync(0xffffffffu, f);
-      if (f) out[pos + __popc(ball & ((1u << lane) - 1u))] = make_int2(a, b);
+      if (f) {
+        const long long at = pos + __popc(ball & ((1u << lane) - 1u));
+        out[at] = make_int2(a, b);
+        if (P.cand_feat) {
+          const long long pg = pmat[static_cast<long long>(a) * g + b];
+          long long denom = old[a] + old[b];
+          if (denom < 1) denom = 1;
+          P.cand_feat[P.cand_off[ri] + at] =
+              make_float2(static_cast<float>(pg), static_cast<float>(static_cast<double>(pg) / denom));
+        }
+      }
       pos += __popc(ball);
     }
   }
@@ -1038,10 +1051,17 @@ __global__ void __launch_bounds__(kSmallWarps * 32) PrepareSmallKernel(PreparePa
   const int total = __shfl_sync(0xffffffffu, ex, 31);
   ex -= cnt;
   int2* out = P.cand + P.cand_off[ri];
+  float2* feat = P.cand_feat ? P.cand_feat + P.cand_off[ri] : nullptr;
   unsigned bits = mine;
   while (bits) {
     const int b = __ffs(bits) - 1;
     bits &= bits - 1;
+    if (feat) {
+      const long long pg = S.p[TriIndex(lane, b, g)];
+      long long denom = S.old[lane] + S.old[b];
+      if (denom < 1) denom = 1;
+      feat[ex] = make_float2(static_cast<float>(pg), static_cast<float>(static_cast<double>(pg) / denom));
+    }
     out[ex++] = make_int2(lane, b);
   }
   examined = static_cast<unsigned long long>(WarpSum(static_cast<long long>(examined)));
@@ -1069,9 +1089,28 @@ struct ScoreParams {
   const int2* cand;
   const int* cand_cnt;
   longlong2* res;
+  // learned ranker (phase 0: off, every slot scored). keep[slot]: 1 =
+  // exploration slot, scored in phase 1; 2 = scored in phase 2 iff its logit
+  // zbuf[slot] >= *cutoff (the cutoff comes from phase 1's passing pairs)
+  int phase;
+  const unsigned char* keep;
+  const float* zbuf;
+  float* zpos;        // phase 1: logits of the exploration pairs passing the filter
+  unsigned* npos;
+  unsigned zcap;
+  const float* cutoff;
+  int audit;          // phase 2: score pruned slots aside and count the ones the filter passes
+  double threshold;
+  int use_threshold;
   unsigned long long* stats;
   DevError* err;
 };
+
+__device__ __forceinline__ bool PassesFilter(long long gain, long long before, double threshold, int use_threshold) {
+  if (gain <= 0) return false;
+  if (!use_threshold) return true;
+  return before > 0 && static_cast<double>(gain) / static_cast<double>(before) >= threshold;
+}
 
 __device__ __forceinline__ void FlushScoreStats(unsigned long long* stats, const GainWork& w, long long pairs,
                                                 long long view_nnz) {
@@ -1088,15 +1127,6 @@ __device__ __forceinline__ void FlushScoreStats(unsigned long long* stats, const
             static_cast<unsigned long long>(8 * (w.raw_a + w.raw_b) + 4 * w.uni + 24 * pairs));
 }
 
-// Index of the real group owning a slot: last ri in [lo, hi) with off[ri] <= slot.
-__device__ __forceinline__ int OwnerOfSlot(const long long* off, int lo, int hi, long long slot) {
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (off[mid] <= slot) lo = mid; else hi = mid;
-  }
-  return lo;
-}
-
 // One warp per candidate slot of the block (the concatenated per-group
 // candidate capacities); slots past a group's candidate count are skipped.
 __global__ void __launch_bounds__(kScoreThreads) ScoreKernel(ScoreParams P) {
@@ -1107,6 +1137,8 @@ __global__ void __launch_bounds__(kScoreThreads) ScoreKernel(ScoreParams P) {
   const long long nw = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
   GainWork w = {0, 0, 0, 0};
   long long pairs = 0, view_nnz = 0;
+  unsigned long long pruned = 0;
+  const float cutoff = P.phase == 2 ? *P.cutoff : 0.0f;
   for (long long slot = s0 + warp; slot < s1; slot += nw) {
     const int ri = OwnerOfSlot(P.cand_off, P.rg0, P.rg0 + P.nrg, slot);
     const int p = static_cast<int>(slot - P.cand_off[ri]);
@@ -1116,14 +1148,44 @@ __global__ void __launch_bounds__(kScoreThreads) ScoreKernel(ScoreParams P) {
     const int a = q[c.x];
     const int b = q[c.y];
     long long gain = 0, before = 0;
+    if (P.phase == 1 && P.keep[slot] != 1) continue;
+    if (P.phase == 2) {
+      if (P.keep[slot] == 1) continue;  // exploration slot, scored in phase 1
+      if (P.zbuf[slot] < cutoff) {
+        // pruned by the ranker: not scored (the audit scores it aside)
+        if (P.audit) {
+          GainWork aw = {0, 0, 0, 0};
+          WarpExactGain(P.Q, a, b, &gain, &before, &aw, P.err);
+          if (lane == 0 && PassesFilter(gain, before, P.threshold, P.use_threshold)) {
+            atomicAdd(&P.stats[kStRkAuditPassing], 1ull);
+            atomicAdd(&P.stats[kStRkAuditLost], 1ull);
+          }
+        }
+        if (lane == 0) {
+          P.res[slot] = make_longlong2(0, -1);
+          ++pruned;
+        }
+        continue;
+      }
+    }
     WarpExactGain(P.Q, a, b, &gain, &before, &w, P.err);
     if (lane == 0) {
+      if (P.phase != 0 && PassesFilter(gain, before, P.threshold, P.use_threshold)) {
+        if (P.audit) atomicAdd(&P.stats[kStRkAuditPassing], 1ull);
+        if (P.phase == 1) {
+          const unsigned at = atomicAdd(P.npos, 1u);
+          if (at < P.zcap) P.zpos[at] = P.zbuf[slot];
+        }
+      }
       P.res[slot] = make_longlong2(gain, before);
       ++pairs;
       view_nnz += P.Q.len[a] + (P.Q.internal[a] > 0 ? 1 : 0) + P.Q.len[b] + (P.Q.internal[b] > 0 ? 1 : 0);
     }
   }
-  if (lane == 0) FlushScoreStats(P.stats, w, pairs, view_nnz);
+  if (lane == 0) {
+    FlushScoreStats(P.stats, w, pairs, view_nnz);
+    if (pruned) atomicAdd(&P.stats[kStRkPruned], pruned);
+  }
 }
 
 // Scoring service over an explicit pair list (ScoreCandidatesCuda's role).
@@ -1245,6 +1307,7 @@ __global__ void __launch_bounds__(kSelectThreads) SelectKernel(SelectParams P) {
     const longlong2 r = P.res[base + c];
     const long long gain = r.x;
     const long long before = r.y;
+    if (before < 0) continue;  // pruned by the ranker before scoring
     if (gain <= 0) {
       ++my_rej;
       continue;
@@ -1752,6 +1815,13 @@ void Engine::PrepareIterationBuffers() {
   const size_t ncand = static_cast<size_t>(h_cand_off_[R]);
   d_cand_.ensure(ncand + 1);
   d_res_.ensure(ncand + 1);
+  if (cfg_.ranker) {
+    d_cand_feat_.ensure(ncand + 1);
+    d_rk_keep_.ensure(ncand + 1);
+    d_rk_zbuf_.ensure(ncand + 1);
+    for (int k = 0; k < 2; ++k) d_rk_zpos_[k].ensure(static_cast<size_t>(RankerExploreCap(static_cast<long long>(ncand))));
+  }
+  rk_iter_slots_ = static_cast<long long>(ncand);
   const size_t nsel = static_cast<size_t>(h_sel_off_[R]);
   d_sel_keep_.ensure(nsel + 1);
   d_sel_rem_.ensure(nsel + 1);
@@ -1840,6 +1910,7 @@ void Engine::LaunchPrepare(int s0, int s1, int b0, int b1) {
   PP.top_k = cfg_.top_k;
   PP.stats = d_stats_.p;
   PP.err = d_err_.p;
+  PP.cand_feat = cfg_.ranker ? d_cand_feat_.p : nullptr;
   BeginTimed(kTimePrepare);
   if (s1 > s0) {
     PP.list = d_small_.p;
@@ -1895,7 +1966,7 @@ void Engine::LaunchPrepare(int s0, int s1, int b0, int b1) {
   EndTimed(kTimePrepare);
 }
 
-void Engine::RunBlock(size_t b, double threshold) {
+void Engine::RunBlock(size_t b, double threshold, int iter, int total_iterations) {
   ++block_stamp_;
   ++hstats_.blocks;
   const int rg0 = h_block_rg_[b];
@@ -1918,11 +1989,38 @@ void Engine::RunBlock(size_t b, double threshold) {
   SP.res = d_res_.p;
   SP.stats = d_stats_.p;
   SP.err = d_err_.p;
+  SP.threshold = threshold;
+  SP.use_threshold = cfg_.ea_use_threshold ? 1 : 0;
+  SP.audit = cfg_.ranker_audit ? 1 : 0;
+  SP.phase = 0;
+  SP.keep = d_rk_keep_.p;
+  SP.zbuf = d_rk_zbuf_.p;
+  SP.zpos = d_rk_zpos_[0].p;
+  SP.npos = d_rk_npos_.p;
+  SP.zcap = 0;
+  SP.cutoff = d_rk_cut_.p;
   const int sgrid = static_cast<int>(std::min<long long>((slots + 7) / 8, 152 * 16));
+  // learned ranker: trained after the logging iterations; afterwards the
+  // exploration subset is scored first, then the rest above the cutoff
+  const bool ranking = cfg_.ranker && rk_trained_ && iter > cfg_.ranker_train_iters;
+  if (ranking) {
+    RankerRank(rg0, nrg, slots, threshold, iter);
+    SP.phase = 1;
+    SP.zcap = static_cast<unsigned>(RankerExploreCap(slots));
+    BeginTimed(kTimeScore);
+    ++launches_;
+    ScoreKernel<<<sgrid, kScoreThreads, 0, stream_>>>(SP);
+    EndTimed(kTimeScore);
+    RankerCutoff(slots);
+    SP.phase = 2;
+  }
   BeginTimed(kTimeScore);
   ++launches_;
   ScoreKernel<<<sgrid, kScoreThreads, 0, stream_>>>(SP);
   EndTimed(kTimeScore);
+  if (cfg_.ranker && !rk_trained_ && iter <= cfg_.ranker_train_iters) {
+    RankerLog(rg0, nrg, slots, iter, threshold, total_iterations);
+  }
   SelectParams LP;
   LP.order = d_order_.p;
   LP.gstart = d_gstart_.p;
@@ -1956,20 +2054,21 @@ void Engine::RunBlock(size_t b, double threshold) {
 }
 
 void Engine::Merge(int iter, int total_iterations) {
-  (void)total_iterations;
   if (n_groups_ < 0) throw std::runtime_error("Merge requires a preceding Divide");
   // ComputeMergeThreshold, reciprocal policy (src/sweg.cpp:400-406)
   const double threshold = 1.0 / static_cast<double>(iter + 1);
   EnsurePoolRoom();
   PrepareIterationBuffers();
   for (size_t b = 0; b + 1 < h_block_rg_.size(); ++b) {
-    if (h_block_rg_[b + 1] > h_block_rg_[b]) RunBlock(b, threshold);
+    if (h_block_rg_[b + 1] > h_block_rg_[b]) RunBlock(b, threshold, iter, total_iterations);
   }
   ++launches_;
   RelabelKernel<<<(n_ + 255) / 256, 256, 0, stream_>>>(d_label_.p, d_fwd_.p, n_);
   n_groups_ = -1;  // the groups are consumed
   CheckCuda(cudaStreamSynchronize(stream_), "merge sync");
   CheckError();
+  if (cfg_.ranker && !rk_trained_ && iter == cfg_.ranker_train_iters) RankerTrain();
+  if (cfg_.ranker && rk_trained_ && iter > cfg_.ranker_train_iters) RankerFinishIteration();
 }
 
 void Engine::ScorePairs(const int32_t* rep_a, const int32_t* rep_b, int64_t count, int64_t* gain,

@@ -109,6 +109,15 @@ class EngineOptions:
     seed: int = 1
     device: int = 0
     verify_cuda_gain: bool = False
+    # learned candidate ranker (off: the reference's method)
+    ranker: bool = False
+    ranker_train_iters: int = 5
+    ranker_recall: float = 0.99
+    ranker_audit: bool = False
+    ranker_max_samples: int = 1 << 18
+    ranker_epochs: int = 4
+    ranker_max_steps: int = 256
+    ranker_lr: float = 3e-3
 
 
 class Engine:
@@ -122,6 +131,9 @@ class Engine:
         cfg.divide_hash_dims, cfg.divide_max_group = o.divide_hash_dims, o.divide_max_group
         cfg.ea_use_threshold, cfg.seed, cfg.device = int(o.ea_use_threshold), o.seed, o.device
         cfg.verify_cuda_gain = int(o.verify_cuda_gain)
+        cfg.ranker, cfg.ranker_train_iters, cfg.ranker_recall = int(o.ranker), o.ranker_train_iters, o.ranker_recall
+        cfg.ranker_audit, cfg.ranker_max_samples = int(o.ranker_audit), o.ranker_max_samples
+        cfg.ranker_epochs, cfg.ranker_max_steps, cfg.ranker_lr = o.ranker_epochs, o.ranker_max_steps, o.ranker_lr
         h = C.c_void_p()
         N.check(N.lib().beam_engine_create(graph.n, graph.arcs, _ptr(graph.row_ptr, C.c_int64),
                                            _ptr(graph.col_idx, C.c_int32), C.byref(cfg), C.byref(h)))
@@ -190,6 +202,11 @@ class Engine:
         N.check(N.lib().beam_engine_merge_pairs(self._h, _ptr(keep, C.c_int32), _ptr(remove, C.c_int32),
                                                 len(keep)))
 
+    def ranker_info(self) -> dict:
+        info = N.RankerInfo()
+        N.check(N.lib().beam_engine_ranker_info(self._h, C.byref(info)))
+        return info.as_dict()
+
     def partition(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
         labels = np.zeros(self.n, np.int32)
         head = np.zeros(self.n, np.int32)
@@ -245,3 +262,30 @@ class Engine:
         out = C.c_int64()
         N.check(N.lib().beam_engine_launch_count(self._h, C.byref(out)))
         return int(out.value)
+
+
+RANKER_FEATURES = 16
+RANKER_PARAMS = 64 * 16 + 64 + 64 + 1
+
+
+def ranker_grad(x, y, params, w=None, device: int = 0) -> tuple[np.ndarray, float, np.ndarray]:
+    """One forward + backward pass of the ranker MLP on the GPU (the
+    library's own kernels): gradient of the mean weighted logistic loss with
+    respect to the fp32 master parameters, the loss, and the logits."""
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.ascontiguousarray(y, np.float32)
+    params = np.ascontiguousarray(params, np.float32)
+    n = len(y)
+    if x.shape != (n, RANKER_FEATURES) or params.shape != (RANKER_PARAMS,):
+        raise ValueError("x must be [n, 16] and params [1153]")
+    wp = None
+    if w is not None:
+        w = np.ascontiguousarray(w, np.float32)
+        wp = w.ctypes.data
+    grad = np.zeros(RANKER_PARAMS, np.float32)
+    logits = np.zeros(n, np.float32)
+    loss = C.c_double()
+    N.check(N.lib().beam_ranker_grad(device, x.ctypes.data, y.ctypes.data, wp, n, params.ctypes.data,
+                                     grad.ctypes.data, C.byref(loss), logits.ctypes.data), "beam_ranker_last_error")
+    return grad, float(loss.value), logits
+

@@ -91,7 +91,15 @@ typedef struct {
   int32_t device;            /* CUDA device ordinal */
   uint64_t seed;             /* --seed [1] */
   int32_t verify_cuda_gain;  /* --verify-cuda-gain: re-score and check every commit */
-  int32_t reserved0;
+  /* Learned candidate ranker (this implementation's own; 0 = the reference's method). */
+  int32_t ranker;              /* 1: prune candidates before exact scoring after training */
+  int32_t ranker_train_iters;  /* iterations whose exact gains are logged for training [5] */
+  float ranker_recall;         /* recall of logged positives kept at the cutoff [0.99] */
+  int32_t ranker_audit;        /* 1: also score pruned pairs aside and count the positives lost */
+  int32_t ranker_max_samples;  /* training log capacity [262144] */
+  int32_t ranker_epochs;       /* passes over the log [4] */
+  int32_t ranker_max_steps;    /* Adam steps at most [256] */
+  float ranker_lr;             /* Adam learning rate [0.003] */
 } beam_engine_config;
 
 /* Counters with the reference's metric names (include/sweg.hpp:221-386). */
@@ -143,6 +151,36 @@ int beam_engine_partition(beam_engine* e, int32_t* labels, int32_t* head, int32_
 int beam_engine_export_row(beam_engine* e, int32_t rep, int32_t* nb, int64_t* cnt, int64_t cap, int64_t* len,
                            int64_t* size, int64_t* internal);
 int beam_engine_get_stats(beam_engine* e, beam_engine_stats* out);
+
+/* Learned candidate ranker of the current run. */
+typedef struct {
+  uint64_t samples;        /* logged (features, label) rows */
+  uint64_t positives;      /* rows labelled positive: exact gain > 0, gain/before >= 1/(iterations+1) */
+  uint64_t train_steps;    /* Adam steps */
+  uint64_t ranked;         /* candidate pairs ranked in the ranking iterations */
+  uint64_t pruned;         /* of which not scored */
+  uint64_t audit_passing;  /* ranker_audit: ranked pairs passing the iteration's threshold filter */
+  uint64_t audit_lost;     /* ranker_audit: pruned pairs among them */
+  double train_ms;         /* training + calibration, host wall time */
+  double first_loss, final_loss;  /* weighted logistic loss of the first and last mini-batch */
+  double cutoff;           /* logit cutoff */
+  double calib_recall;     /* recall of the logged positives at the cutoff */
+  double calib_prune;      /* fraction of the log below the cutoff */
+  int32_t trained;
+  int32_t reserved;
+} beam_ranker_info;
+int beam_engine_ranker_info(beam_engine* e, beam_ranker_info* out);
+
+/* One forward + backward pass of the ranker's MLP on `device` over n samples
+ * (x[n][16] features used as given, y[n] labels in {0,1}, w[n] sample
+ * weights or NULL for 1): params[1153] = W1[64][16] | b1[64] | w2[64] | b2
+ * (fp32 master; the forward pass uses the weights rounded to bf16). Writes
+ * the gradient of the mean weighted logistic loss w.r.t. params, the loss
+ * and (if logits != NULL) the n logits. The gradient check against the CPU
+ * oracle runs through this entry. */
+int beam_ranker_grad(int32_t device, const float* x, const float* y, const float* w, int64_t n,
+                     const float* params, float* grad, double* loss, float* logits);
+const char* beam_ranker_last_error(void);
 /* QuotientGraph::Nnz (src/quotient_graph.cpp:259-270). */
 int beam_engine_quotient_nnz(beam_engine* e, int64_t* nnz);
 /* CUDA-event timing of every launch of one kernel class (BEAM_TIME_*). */
