@@ -7,11 +7,11 @@ is reset to singletons and L2 is flushed (256 MB write) before every timed
 step; both stay outside the timed span, which is measured with CUDA events on
 the engine's stream. value = accepted merges of all ranks / slowest rank's
 time for the headline form (--form, default batched: one block of all groups
-per iteration); the other form (plain: the reference's 64-group blocks,
-bit-exact with the reference) is timed beside it for the speed-up and the
-cost-ratio comparison. e2e runs the public C ABI from host buffers every step
-(create from the host CSR = H2D copies, 20 iterations, partition download =
-D2H).
+per iteration); the other forms (plain: the reference's 64-group blocks,
+bit-exact with the reference; ranker: batched + the learned candidate
+ranker) are timed beside it for the speed-ups and the cost-ratio comparison.
+e2e runs the public C ABI from host buffers every step (create from the host
+CSR = H2D copies, 20 iterations, partition download = D2H).
 
 --impl reference times the CPU implementation of the path (the C oracle,
 a restatement of the reference pinned to its outputs) on the host cores.
@@ -156,15 +156,23 @@ def measured_peak() -> tuple[float, str]:
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def profiled_traffic(kernel: str) -> float | None:
-    """DRAM bytes per launch from the committed ncu summary of this kernel."""
-    for f in sorted((ROOT / "profiles").glob(f"{kernel}*.md")):
-        for line in f.read_text().splitlines():
-            if line.strip().startswith("traffic_bytes_per_launch:"):
-                try:
-                    return float(line.split(":", 1)[1].strip().split()[0])
-                except ValueError:
-                    return None
+# the kernel that each timed class stands for (its largest kernel)
+KERNEL_OF_CLASS = {"score": "ScoreKernel", "prepare": "PrepareKernel", "update": "CommitKernel",
+                   "divide": "MinHashKernel"}
+
+
+def profiled_traffic(kernel_class: str, workload: str, form: str) -> float | None:
+    """Mean DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)
+    from the committed ncu summary of this kernel on this workload and form."""
+    f = ROOT / "profiles" / f"{KERNEL_OF_CLASS[kernel_class]}_{workload}_{form}_dram.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
     return None
 
 
@@ -182,16 +190,19 @@ def golden_hash(workload: str) -> str | None:
 FORMS = {
     # one block per iteration: every group of an iteration is prepared, scored,
     # selected and committed by one launch of each kernel
-    "batched": 1 << 30,
+    "batched": {"group_batch_size": 1 << 30},
+    # the batched form with the learned candidate ranker (trained on the exact
+    # gains of iterations 1-5, prunes candidates before exact scoring later)
+    "ranker": {"group_batch_size": 1 << 30, "ranker": True},
     # the reference's 64-group blocks: bit-exact with the reference CPU path
-    "plain": 64,
+    "plain": {"group_batch_size": 64},
 }
 
 
 def form_engine(g, device: int, form: str):
     from beam_gb300 import Engine
 
-    return Engine(g, device=device, ea_use_threshold=True, group_batch_size=FORMS[form])
+    return Engine(g, device=device, ea_use_threshold=True, **FORMS[form])
 
 
 def kernel_breakdown(e) -> dict:
@@ -253,7 +264,7 @@ def run_ours(args, dist: Dist) -> dict | None:
     log(f"[bench] graph {args.workload}: n={g.n} m={g.edges} ({time.perf_counter() - t0:.1f}s)")
     device = dist.local_rank
     head_form = args.form
-    other_form = "plain" if head_form == "batched" else "batched"
+    others = [] if args.no_other_form else [f for f in FORMS if f != head_form]
     want = golden_hash(args.workload)
 
     # headline form: warm-up, kernel breakdown, timed region
@@ -262,7 +273,9 @@ def run_ours(args, dist: Dist) -> dict | None:
         e.reset()
         e.run(ITERATIONS)
     breakdown = kernel_breakdown(e)
-    dominant = args.timed_kernel or max(breakdown, key=lambda k: breakdown[k]["ms"])
+    # the roofline kernel: ScoreKernel, the largest single kernel of the run
+    # (the prepare class is larger in total but spans six kernels and a sort)
+    dominant = args.timed_kernel or "score"
     dist.barrier()
     e.synchronize()
     clock_log = ROOT / "gpurun_out" / "bench_clocks.csv" if (ROOT / "gpurun_out").exists() else None
@@ -282,11 +295,10 @@ def run_ours(args, dist: Dist) -> dict | None:
                          "merges_per_s": round(value / dist.world, 1),
                          "merges_per_step": t["merges"] // max(1, args.steps),
                          "cost_ratio_mags_compatible": round(head_ratio, 6),
-                         "partition_hash": head_hash,
-                         "group_batch_size": FORMS[head_form]}}
+                         "partition_hash": head_hash, **FORMS[head_form]}}
 
-    # the other form, for the speed-up and the cost-ratio comparison
-    if not args.no_other_form:
+    # the other forms, for the speed-ups and the cost-ratio comparison
+    for other_form in others:
         eo = form_engine(g, device, other_form)
         eo.reset()
         eo.run(ITERATIONS)
@@ -294,22 +306,26 @@ def run_ours(args, dist: Dist) -> dict | None:
         to = timed_steps(eo, o_steps, None)
         o_ms = sum(to["step_ms"]) / o_steps
         o_ratio, o_hash = final_cost_ratio(eo, g)
+        info = eo.ranker_info() if FORMS[other_form].get("ranker") else None
         eo.close()
         forms[other_form] = {"wall_s_20iter": round(o_ms / 1000.0, 4),
                              "merges_per_s": round(to["merges"] / (sum(to["step_ms"]) / 1000.0), 1),
                              "merges_per_step": to["merges"] // o_steps,
                              "cost_ratio_mags_compatible": round(o_ratio, 6),
-                             "partition_hash": o_hash,
-                             "group_batch_size": FORMS[other_form], "steps": o_steps}
+                             "partition_hash": o_hash, "steps": o_steps, **FORMS[other_form]}
+        if info:
+            forms[other_form]["ranker"] = {k: info[k] for k in ("samples", "train_steps", "ranked", "pruned",
+                                                                "train_ms", "final_loss")}
     if "plain" in forms:
         forms["plain"]["bit_exact_vs_reference"] = None if want is None else forms["plain"]["partition_hash"] == want
-    comparison = None
-    if "plain" in forms and "batched" in forms:
-        comparison = {
-            "speedup_batched_vs_plain": round(forms["plain"]["wall_s_20iter"] / forms["batched"]["wall_s_20iter"], 3),
-            "cost_ratio_delta_abs": round(forms["batched"]["cost_ratio_mags_compatible"]
-                                          - forms["plain"]["cost_ratio_mags_compatible"], 6),
-        }
+    comparison = {}
+    if "plain" in forms:
+        for f in forms:
+            if f == "plain":
+                continue
+            comparison[f"speedup_{f}_vs_plain"] = round(forms["plain"]["wall_s_20iter"] / forms[f]["wall_s_20iter"], 3)
+            comparison[f"cost_ratio_delta_abs_{f}_vs_plain"] = round(
+                forms[f]["cost_ratio_mags_compatible"] - forms["plain"]["cost_ratio_mags_compatible"], 6)
 
     # e2e through the C ABI from host buffers: create from the host CSR
     # (H2D), 20 iterations, partition download (D2H)
@@ -329,7 +345,7 @@ def run_ours(args, dist: Dist) -> dict | None:
     peak, peak_kind = measured_peak()
     kernel_ms, kernel_launches = t["kernel_ms"], t["kernel_launches"]
     achieved = t["kernel_bytes"] / (kernel_ms / 1000.0) / 1e9 if kernel_ms > 0 else 0.0
-    traffic = profiled_traffic(dominant)
+    traffic = profiled_traffic(dominant, args.workload, head_form)
     result = {
         "metric": METRIC,
         "value": round(value, 1),
@@ -346,8 +362,9 @@ def run_ours(args, dist: Dist) -> dict | None:
         "config": {
             "workload": f"{args.workload}: {WORKLOAD_DESC.get(args.workload, spec)}; n={g.n}, m={g.edges}",
             "form": head_form,
-            "path": ("batched GPU form: one block of all groups per iteration"
-                     if head_form == "batched" else "plain GPU form: 64-group blocks, bit-exact with the reference"),
+            "path": {"batched": "batched GPU form: one block of all groups per iteration",
+                     "ranker": "batched GPU form + learned candidate ranker",
+                     "plain": "plain GPU form: 64-group blocks, bit-exact with the reference"}[head_form],
             "flags": "batch-ea-blocked, mags-compatible, persistent, incremental, legacy index, certification off, "
                      "g0, top-k 16, reciprocal threshold, 20 iterations, seed 1",
             "wall_s_20iter": round(ms_per_step / 1000.0, 4),
@@ -365,7 +382,7 @@ def run_ours(args, dist: Dist) -> dict | None:
         },
         "gpu_launches": t["launches"],
         "roofline": {
-            "kernel": dominant,
+            "kernel": KERNEL_OF_CLASS[dominant],
             "bound": "hbm",
             "achieved": round(achieved, 2),
             "peak": peak,
@@ -447,8 +464,8 @@ def profile_run(args) -> None:
     from beam_gb300 import WORKLOADS, Engine, Graph
 
     g = Graph.generate(WORKLOADS[args.workload])
-    batch = (1 << 30) if args.batched else 64
-    with Engine(g, ea_use_threshold=True, group_batch_size=batch) as e:
+    batch = FORMS[args.form]["group_batch_size"]
+    with Engine(g, ea_use_threshold=True, **FORMS[args.form]) as e:
         t = time.perf_counter()
         e.run(ITERATIONS)
         e.synchronize()
@@ -462,7 +479,6 @@ def profile_run(args) -> None:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile-run", action="store_true", help="one run only, for ncu")
-    ap.add_argument("--batched", action="store_true", help="with --profile-run: one block per iteration")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
@@ -472,7 +488,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--form", choices=list(FORMS), default="batched",
                     help="form whose throughput is the headline value")
-    ap.add_argument("--no-other-form", action="store_true", help="skip timing the other form")
+    ap.add_argument("--no-other-form", action="store_true", help="skip timing the other forms")
     args = ap.parse_args()
     if args.profile_run:
         profile_run(args)
