@@ -60,12 +60,18 @@ struct GainWork {
   long long raw_a, raw_b, uni, ovl;
 };
 
-// Warp-cooperative ExactMergeGainPersistentImpl: lanes walk row a and look
-// each neighbour up in row b (shared neighbours give two before-terms), then
-// walk row b and keep the neighbours row a lacks; e(a,b) is read from both
-// rows and must agree. Every term is exact int64.
+// Warp-cooperative ExactMergeGainPersistentImpl as a tiled merge of the two
+// sorted rows: each step loads the next 32 entries of both rows (coalesced);
+// with lim = the smaller of the two tiles' last neighbours, every entry <= lim
+// is final in this step (an equal neighbour in the other row, if any, is in
+// the other tile), and each lane finds its entry in the other tile by a
+// 5-step shuffle search. Shared neighbours give two before-terms, one-sided
+// neighbours one; e(a,b) is read from both rows and must agree. Every term
+// is exact int64; the work is O(|R_a| + |R_b|).
 __device__ void WarpExactGain(const QuotientView& Q, int a, int b, long long* gain_out, long long* before_out,
                               GainWork* work, DevError* err) {
+  constexpr unsigned kFull = 0xffffffffu;
+  constexpr Entry kPadEntry = static_cast<Entry>(0x7fffffffull) << 32;  // neighbour INT_MAX, count 0
   const int lane = threadIdx.x & 31;
   const long long sa = Q.size[a];
   const long long sb = Q.size[b];
@@ -76,38 +82,61 @@ __device__ void WarpExactGain(const QuotientView& Q, int a, int b, long long* ga
   const int lb = Q.len[b];
   long long before = 0, after = 0, eab_a = 0, eab_b = 0;
   int uni = 0, ovl = 0, bad = 0;
-  for (int i = lane; i < la; i += 32) {
-    const Entry e = ra[i];
-    const int x = EntNb(e);
-    const long long ea = EntCnt(e);
-    if (x == b) {
-      eab_a = ea;
-      continue;
+  int pa = 0, pb = 0;
+  while (pa < la || pb < lb) {
+    const bool va = pa + lane < la;
+    const bool vb = pb + lane < lb;
+    const Entry ea_e = va ? ra[pa + lane] : kPadEntry;
+    const Entry eb_e = vb ? rb[pb + lane] : kPadEntry;
+    const int xa = EntNb(ea_e);
+    const int xb = EntNb(eb_e);
+    const int last_a = __shfl_sync(kFull, xa, 31);
+    const int last_b = __shfl_sync(kFull, xb, 31);
+    const int lim = last_a < last_b ? last_a : last_b;
+    // lower bound of xa in the b tile and of xb in the a tile
+    int pos_b = 0, pos_a = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+      const int probe_b = __shfl_sync(kFull, xb, pos_b + step - 1);
+      const int probe_a = __shfl_sync(kFull, xa, pos_a + step - 1);
+      if (probe_b < xa) pos_b += step;
+      if (probe_a < xb) pos_a += step;
     }
-    const long long eb = RowLookup(rb, lb, x);
-    const long long sx = Q.size[x];
-    if (eb != 0) {
-      before += BlockCost(sa, sx, ea, false, bad) + BlockCost(sb, sx, eb, false, bad);
-      ++ovl;
-    } else {
-      before += BlockCost(sa, sx, ea, false, bad);
+    const Entry cand_b = __shfl_sync(kFull, eb_e, pos_b);
+    const Entry cand_a = __shfl_sync(kFull, ea_e, pos_a);
+    const bool fin_a = va && xa <= lim;
+    const bool fin_b = vb && xb <= lim;
+    if (fin_a) {
+      const long long ca = EntCnt(ea_e);
+      if (xa == b) {
+        eab_a = ca;
+      } else {
+        const long long sx = Q.size[xa];
+        if (EntNb(cand_b) == xa) {
+          const long long cb = EntCnt(cand_b);
+          before += BlockCost(sa, sx, ca, false, bad) + BlockCost(sb, sx, cb, false, bad);
+          after += BlockCost(sw, sx, ca + cb, false, bad);
+          ++ovl;
+        } else {
+          before += BlockCost(sa, sx, ca, false, bad);
+          after += BlockCost(sw, sx, ca, false, bad);
+        }
+        ++uni;
+      }
     }
-    after += BlockCost(sw, sx, ea + eb, false, bad);
-    ++uni;
-  }
-  for (int j = lane; j < lb; j += 32) {
-    const Entry e = rb[j];
-    const int x = EntNb(e);
-    const long long eb = EntCnt(e);
-    if (x == a) {
-      eab_b = eb;
-      continue;
+    if (fin_b) {
+      const long long cb = EntCnt(eb_e);
+      if (xb == a) {
+        eab_b = cb;
+      } else if (EntNb(cand_a) != xb) {
+        const long long sx = Q.size[xb];
+        before += BlockCost(sb, sx, cb, false, bad);
+        after += BlockCost(sw, sx, cb, false, bad);
+        ++uni;
+      }
     }
-    if (RowLookup(ra, la, x) != 0) continue;
-    const long long sx = Q.size[x];
-    before += BlockCost(sb, sx, eb, false, bad);
-    after += BlockCost(sw, sx, eb, false, bad);
-    ++uni;
+    pa += __popc(__ballot_sync(kFull, fin_a));
+    pb += __popc(__ballot_sync(kFull, fin_b));
   }
   before = WarpSum(before);
   after = WarpSum(after);
@@ -115,7 +144,7 @@ __device__ void WarpExactGain(const QuotientView& Q, int a, int b, long long* ga
   eab_b = WarpMax(eab_b);
   uni = WarpSumInt(uni);
   ovl = WarpSumInt(ovl);
-  bad = __any_sync(0xffffffffu, bad);
+  bad = __any_sync(kFull, bad);
   if (eab_a != eab_b) {
     if (lane == 0) RaiseError(err, kErrAsymmetric, a, b, 0);
   }
@@ -189,6 +218,7 @@ struct PrepareParams {
   const long long* moff;  // member-count prefix over the big-group list
   BigDesc* desc;          // per big-group list entry
   float2* cand_feat;      // per candidate: proxy gain, proxy ratio (ranker features; nullptr: off)
+  int2* cand_rep;         // per candidate slot: the pair's supernode ids (unused slots stay -1)
   const long long* soff;  // sort-slot prefix over the big-group list (0 slots: not deferred)
   long long slot0;        // soff of the launch's first entry
   unsigned long long* skey;  // unsorted keys / values of the launch's slots
@@ -600,143 +630,134 @@ __global__ void __launch_bounds__(256) PrepareMembersKernel(PrepareParams P) {
   const int* q = P.order + P.gstart[gid];
   const long long gg = static_cast<long long>(g) * g;
   unsigned char* mat = P.mat + P.mat_off[ri];
-  long long* pmat = reinterpret_cast<long long*>(mat);
-  double* rmat = reinterpret_cast<double*>(mat + 8 * gg);
-  int* cmat = reinterpret_cast<int*>(mat + 16 * gg);
+  const long long* pmat = reinterpret_cast<const long long*>(mat);
   unsigned char* fmat = mat + 20 * gg;
   const long long* old = reinterpret_cast<const long long*>(mat + OldCostOffset(gg));
-  // per member: candidates with positive proxy, ratio, top-k
+  // per member: candidates with positive proxy, ratio, top-k (the ratio is
+  // recomputed where it is needed instead of being stored)
   int top_k = P.top_k < g - 1 ? P.top_k : g - 1;
   if (top_k < 1) top_k = 1;
-  {
-    int cnt = 0;
-    double* rrow = rmat + static_cast<long long>(i) * g;
-    int* crow = cmat + static_cast<long long>(i) * g;
-    const long long* prow = pmat + static_cast<long long>(i) * g;
-#pragma unroll 4
-    for (int base = 0; base < g; base += 32) {
-      const int j = base + lane;
-      const long long pg = (j < g && j != i) ? prow[j] : 0;
-      const bool pred = pg > 0;
-      const unsigned ball = __ballot_sync(0xffffffffu, pred);
-      if (pred) {
-        const int pos = cnt + __popc(ball & ((1u << lane) - 1u));
-        const int a = i < j ? i : j;
-        const int b = i < j ? j : i;
-        long long denom = old[a] + old[b];
-        if (denom < 1) denom = 1;
-        rrow[pos] = static_cast<double>(pg) / static_cast<double>(denom);
-        crow[pos] = j;
-      }
-      cnt += __popc(ball);
+  const long long* prow = pmat + static_cast<long long>(i) * g;
+  const long long old_i = old[i];
+  auto ratio_of = [&](int j, long long pg) {
+    long long denom = old_i + old[j];
+    if (denom < 1) denom = 1;
+    return static_cast<double>(pg) / static_cast<double>(denom);
+  };
+  int cnt = 0;
+  for (int base = 0; base < g; base += 32) {
+    const int j = base + lane;
+    const bool pred = j < g && j != i && prow[j] > 0;
+    cnt += __popc(__ballot_sync(0xffffffffu, pred));
+  }
+  const int qi = q[i];
+  if (cnt <= top_k) {
+    for (int j = lane; j < g; j += 32) {
+      if (j == i || prow[j] <= 0) continue;
+      const int a = i < j ? i : j;
+      const int b = i < j ? j : i;
+      fmat[static_cast<long long>(a) * g + b] = 1;
     }
-    __syncwarp();
-    const int qi = q[i];
-    if (cnt <= top_k) {
-      for (int c = lane; c < cnt; c += 32) {
-        const int j = crow[c];
-        const int a = i < j ? i : j;
-        const int b = i < j ? j : i;
+  } else if (top_k <= kLaneTopK) {
+    // each lane keeps its best top_k candidates sorted, then the warp merges
+    // the 32 lists head by head (candidates are distinct, so no key ties)
+    RankKey lst[kLaneTopK];
+    int nl = 0;
+    for (int j = lane; j < g; j += 32) {
+      if (j == i) continue;
+      const long long pg = prow[j];
+      if (pg <= 0) continue;
+      RankKey k;
+      k.j = j;
+      k.ratio = ratio_of(j, pg);
+      k.pg = pg;
+      const int qj = q[j];
+      k.lo = qi < qj ? qi : qj;
+      k.hi = qi < qj ? qj : qi;
+      if (nl == top_k && !Better(k, lst[nl - 1])) continue;
+      int pos = nl < top_k ? nl : top_k - 1;
+      while (pos > 0 && Better(k, lst[pos - 1])) {
+        lst[pos] = lst[pos - 1];
+        --pos;
+      }
+      lst[pos] = k;
+      if (nl < top_k) ++nl;
+    }
+    int head = 0;
+    for (int r = 0; r < top_k; ++r) {
+      RankKey best;
+      bool have = head < nl;
+      if (have) best = lst[head];
+      int src = lane;
+      for (int o = 16; o > 0; o >>= 1) {
+        RankKey other;
+        other.ratio = __shfl_xor_sync(0xffffffffu, best.ratio, o);
+        other.pg = __shfl_xor_sync(0xffffffffu, best.pg, o);
+        other.lo = __shfl_xor_sync(0xffffffffu, best.lo, o);
+        other.hi = __shfl_xor_sync(0xffffffffu, best.hi, o);
+        other.j = __shfl_xor_sync(0xffffffffu, best.j, o);
+        const int osrc = __shfl_xor_sync(0xffffffffu, src, o);
+        const int ohave = __shfl_xor_sync(0xffffffffu, have ? 1 : 0, o);
+        if (ohave && (!have || Better(other, best))) {
+          best = other;
+          have = true;
+          src = osrc;
+        }
+      }
+      if (!have) break;
+      if (src == lane) ++head;
+      if (lane == 0) {
+        const int a = i < best.j ? i : best.j;
+        const int b = i < best.j ? best.j : i;
         fmat[static_cast<long long>(a) * g + b] = 1;
       }
-    } else if (top_k <= kLaneTopK) {
-      // each lane keeps its best top_k candidates sorted, then the warp merges
-      // the 32 lists head by head (candidates are distinct, so no key ties)
-      RankKey lst[kLaneTopK];
-      int nl = 0;
-      for (int c = lane; c < cnt; c += 32) {
+    }
+  } else {
+    RankKey prev;
+    bool have_prev = false;
+    for (int r = 0; r < top_k; ++r) {
+      RankKey best;
+      bool have = false;
+      for (int j = lane; j < g; j += 32) {
+        if (j == i) continue;
+        const long long pg = prow[j];
+        if (pg <= 0) continue;
         RankKey k;
-        k.j = crow[c];
-        k.ratio = rrow[c];
-        k.pg = prow[k.j];
-        const int qj = q[k.j];
+        k.j = j;
+        k.ratio = ratio_of(j, pg);
+        k.pg = pg;
+        const int qj = q[j];
         k.lo = qi < qj ? qi : qj;
         k.hi = qi < qj ? qj : qi;
-        if (nl == top_k && !Better(k, lst[nl - 1])) continue;
-        int pos = nl < top_k ? nl : top_k - 1;
-        while (pos > 0 && Better(k, lst[pos - 1])) {
-          lst[pos] = lst[pos - 1];
-          --pos;
-        }
-        lst[pos] = k;
-        if (nl < top_k) ++nl;
-      }
-      int head = 0;
-      for (int r = 0; r < top_k; ++r) {
-        RankKey best;
-        bool have = head < nl;
-        if (have) best = lst[head];
-        int src = lane;
-        for (int o = 16; o > 0; o >>= 1) {
-          RankKey other;
-          other.ratio = __shfl_xor_sync(0xffffffffu, best.ratio, o);
-          other.pg = __shfl_xor_sync(0xffffffffu, best.pg, o);
-          other.lo = __shfl_xor_sync(0xffffffffu, best.lo, o);
-          other.hi = __shfl_xor_sync(0xffffffffu, best.hi, o);
-          other.j = __shfl_xor_sync(0xffffffffu, best.j, o);
-          const int osrc = __shfl_xor_sync(0xffffffffu, src, o);
-          const int ohave = __shfl_xor_sync(0xffffffffu, have ? 1 : 0, o);
-          if (ohave && (!have || Better(other, best))) {
-            best = other;
-            have = true;
-            src = osrc;
-          }
-        }
-        if (!have) break;
-        if (src == lane) ++head;
-        if (lane == 0) {
-          const int a = i < best.j ? i : best.j;
-          const int b = i < best.j ? best.j : i;
-          fmat[static_cast<long long>(a) * g + b] = 1;
+        if (have_prev && !Better(prev, k)) continue;
+        if (!have || Better(k, best)) {
+          best = k;
+          have = true;
         }
       }
-    } else {
-      RankKey prev;
-      bool have_prev = false;
-      for (int r = 0; r < top_k; ++r) {
-        RankKey best;
-        bool have = false;
-        for (int c = lane; c < cnt; c += 32) {
-          RankKey k;
-          k.j = crow[c];
-          const int a = i < k.j ? i : k.j;
-          const int b = i < k.j ? k.j : i;
-          k.ratio = rrow[c];
-          k.pg = pmat[static_cast<long long>(a) * g + b];
-          const int qj = q[k.j];
-          k.lo = qi < qj ? qi : qj;
-          k.hi = qi < qj ? qj : qi;
-          if (have_prev && !Better(prev, k)) continue;
-          if (!have || Better(k, best)) {
-            best = k;
-            have = true;
-          }
+      for (int o = 16; o > 0; o >>= 1) {
+        RankKey other;
+        other.ratio = __shfl_xor_sync(0xffffffffu, best.ratio, o);
+        other.pg = __shfl_xor_sync(0xffffffffu, best.pg, o);
+        other.lo = __shfl_xor_sync(0xffffffffu, best.lo, o);
+        other.hi = __shfl_xor_sync(0xffffffffu, best.hi, o);
+        other.j = __shfl_xor_sync(0xffffffffu, best.j, o);
+        const int ohave = __shfl_xor_sync(0xffffffffu, have ? 1 : 0, o);
+        if (ohave && (!have || Better(other, best))) {
+          best = other;
+          have = true;
         }
-        for (int o = 16; o > 0; o >>= 1) {
-          RankKey other;
-          other.ratio = __shfl_xor_sync(0xffffffffu, best.ratio, o);
-          other.pg = __shfl_xor_sync(0xffffffffu, best.pg, o);
-          other.lo = __shfl_xor_sync(0xffffffffu, best.lo, o);
-          other.hi = __shfl_xor_sync(0xffffffffu, best.hi, o);
-          other.j = __shfl_xor_sync(0xffffffffu, best.j, o);
-          const int ohave = __shfl_xor_sync(0xffffffffu, have ? 1 : 0, o);
-          if (ohave && (!have || Better(other, best))) {
-            best = other;
-            have = true;
-          }
-        }
-        if (!have) break;
-        if (lane == 0) {
-          const int a = i < best.j ? i : best.j;
-          const int b = i < best.j ? best.j : i;
-          fmat[static_cast<long long>(a) * g + b] = 1;
-        }
-        prev = best;
-        have_prev = true;
       }
+      if (!have) break;
+      if (lane == 0) {
+        const int a = i < best.j ? i : best.j;
+        const int b = i < best.j ? best.j : i;
+        fmat[static_cast<long long>(a) * g + b] = 1;
+      }
+      prev = best;
+      have_prev = true;
     }
   }
-  __syncthreads();
 }
 
 // Output pass of the big groups: the union of kept pairs in (a_idx, b_idx)
@@ -757,6 +778,7 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareOutputKernel(PrepareParam
   const unsigned char* fmat = P.mat + P.mat_off[ri] + 20 * gg;
   const long long* pmat = reinterpret_cast<const long long*>(P.mat + P.mat_off[ri]);
   const long long* old = reinterpret_cast<const long long*>(P.mat + P.mat_off[ri] + OldCostOffset(gg));
+  const int* q = P.order + P.gstart[gid];
   // union of kept pairs in (a_idx, b_idx) order
   for (int a = warp; a < g; a += nwarps) {
     int cnt = 0;
@@ -792,6 +814,7 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareOutputKernel(PrepareParam
       if (f) {
         const long long at = pos + __popc(ball & ((1u << lane) - 1u));
         out[at] = make_int2(a, b);
+        P.cand_rep[P.cand_off[ri] + at] = make_int2(q[a], q[b]);
         if (P.cand_feat) {
           const long long pg = pmat[static_cast<long long>(a) * g + b];
           long long denom = old[a] + old[b];
@@ -1062,6 +1085,7 @@ __global__ void __launch_bounds__(kSmallWarps * 32) PrepareSmallKernel(PreparePa
       if (denom < 1) denom = 1;
       feat[ex] = make_float2(static_cast<float>(pg), static_cast<float>(static_cast<double>(pg) / denom));
     }
+    P.cand_rep[P.cand_off[ri] + ex] = make_int2(S.q[lane], S.q[b]);
     out[ex++] = make_int2(lane, b);
   }
   examined = static_cast<unsigned long long>(WarpSum(static_cast<long long>(examined)));
@@ -1088,6 +1112,7 @@ struct ScoreParams {
   const long long* cand_off;
   const int2* cand;
   const int* cand_cnt;
+  const int2* cand_rep;  // the pair's supernode ids, -1 for unused slots
   longlong2* res;
   // learned ranker (phase 0: off, every slot scored). keep[slot]: 1 =
   // exploration slot, scored in phase 1; 2 = scored in phase 2 iff its logit
@@ -1128,7 +1153,8 @@ __device__ __forceinline__ void FlushScoreStats(unsigned long long* stats, const
 }
 
 // One warp per candidate slot of the block (the concatenated per-group
-// candidate capacities); slots past a group's candidate count are skipped.
+// candidate capacities); slots past a group's candidate count hold -1 and
+// are skipped.
 __global__ void __launch_bounds__(kScoreThreads) ScoreKernel(ScoreParams P) {
   const long long s0 = P.cand_off[P.rg0];
   const long long s1 = P.cand_off[P.rg0 + P.nrg];
@@ -1140,13 +1166,10 @@ __global__ void __launch_bounds__(kScoreThreads) ScoreKernel(ScoreParams P) {
   unsigned long long pruned = 0;
   const float cutoff = P.phase == 2 ? *P.cutoff : 0.0f;
   for (long long slot = s0 + warp; slot < s1; slot += nw) {
-    const int ri = OwnerOfSlot(P.cand_off, P.rg0, P.rg0 + P.nrg, slot);
-    const int p = static_cast<int>(slot - P.cand_off[ri]);
-    if (p >= P.cand_cnt[ri]) continue;
-    const int* q = P.order + P.gstart[P.real[ri]];
-    const int2 c = P.cand[slot];
-    const int a = q[c.x];
-    const int b = q[c.y];
+    const int2 ab = P.cand_rep[slot];
+    if (ab.x < 0) continue;  // past the group's candidate count
+    const int a = ab.x;
+    const int b = ab.y;
     long long gain = 0, before = 0;
     if (P.phase == 1 && P.keep[slot] != 1) continue;
     if (P.phase == 2) {
@@ -1240,6 +1263,9 @@ struct SelectParams {
   BlockCtl* ctl;
   unsigned long long* stats;
   DevError* err;
+  const int* list;  // real-group positions handled by this launch
+  int list0;
+  int nlist;
 };
 
 // In-place ascending bitonic sort of n (power of two) keys by one CTA.
@@ -1277,7 +1303,7 @@ __global__ void __launch_bounds__(kSelectThreads) SelectKernel(SelectParams P) {
   __shared__ unsigned long long* gkeys;
   __shared__ unsigned long long rej_thr, positive;
   const int tid = threadIdx.x;
-  const int ri = P.rg0 + blockIdx.x;
+  const int ri = P.list[P.list0 + blockIdx.x];
   const int gid = P.real[ri];
   const int g = P.glen[gid];
   const int cnt = g >= 2 && g <= kMaxGroup ? P.cand_cnt[ri] : 0;
@@ -1384,6 +1410,127 @@ __global__ void __launch_bounds__(kSelectThreads) SelectKernel(SelectParams P) {
     atomicAdd(&P.stats[kStValidationCalls], static_cast<unsigned long long>(ns));
     atomicAdd(&P.stats[kStValidationWork], work);
     atomicAdd(&P.stats[kStIsolatedGain], static_cast<unsigned long long>(total));
+  }
+}
+
+// Groups of at most kSelectSmallGroup members (at most 28 candidates): one
+// warp per group, one candidate per lane, a register bitonic sort across the
+// lanes and the greedy pass over shuffled keys; counters are summed per CTA.
+// Output and counters equal those of SelectKernel.
+constexpr int kSelectSmallGroup = 8;
+constexpr int kSelectSmallWarps = 8;
+
+__device__ __forceinline__ unsigned long long WarpBitonicSortAsc(unsigned long long key, int lane) {
+  for (int k = 2; k <= 32; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const unsigned long long other = __shfl_xor_sync(0xffffffffu, key, j);
+      const bool up = (lane & k) == 0;
+      const bool lower = (lane & j) == 0;
+      // the lower lane of a pair keeps the smaller key in an ascending run
+      const bool take_min = lower == up;
+      key = take_min ? (other < key ? other : key) : (other > key ? other : key);
+    }
+  }
+  return key;
+}
+
+__global__ void __launch_bounds__(kSelectSmallWarps * 32) SelectSmallKernel(SelectParams P) {
+  __shared__ unsigned long long acc[9];
+  const int lane = threadIdx.x & 31;
+  const int li = blockIdx.x * kSelectSmallWarps + (threadIdx.x >> 5);
+  if (threadIdx.x < 9) acc[threadIdx.x] = 0;
+  __syncthreads();
+  if (li < P.nlist) {
+    const int ri = P.list[P.list0 + li];
+    const int gid = P.real[ri];
+    const int g = P.glen[gid];
+    const int cnt = P.cand_cnt[ri];
+    const long long base = P.cand_off[ri];
+    unsigned long long key = ~0ull;
+    int rej = 0, pos = 0;
+    if (lane < cnt) {
+      const longlong2 r = P.res[base + lane];
+      const long long gain = r.x;
+      const long long before = r.y;
+      if (before >= 0) {  // negative: pruned by the ranker before scoring
+        bool ok = gain > 0;
+        if (ok && P.use_threshold) {
+          ok = before > 0 && static_cast<double>(gain) / static_cast<double>(before) >= P.threshold;
+        }
+        if (!ok) {
+          rej = 1;
+        } else {
+          pos = 1;
+          if (gain > kKeyGainMax) RaiseError(P.err, kErrKeyRange, gid, lane, 0);
+          const int2 ab = P.cand[base + lane];
+          key = (static_cast<unsigned long long>(kKeyGainMax - gain) << (2 * kKeyIdxBits)) |
+                (static_cast<unsigned long long>(ab.x) << kKeyIdxBits) | static_cast<unsigned long long>(ab.y);
+        }
+      }
+    }
+    const int m = __popc(__ballot_sync(0xffffffffu, pos != 0));
+    const int nrej = __popc(__ballot_sync(0xffffffffu, rej != 0));
+    key = WarpBitonicSortAsc(key, lane);
+    const int* q = P.order + P.gstart[gid];
+    const long long so = P.sel_off[ri];
+    const unsigned long long idx_mask = (1ull << kKeyIdxBits) - 1;
+    unsigned used = 0;
+    int ns = 0;
+    long long total = 0;
+    unsigned long long overlap = 0, work = 0;
+    for (int k = 0; k < m; ++k) {
+      const unsigned long long kk = __shfl_sync(0xffffffffu, key, k);
+      const int b = static_cast<int>(kk & idx_mask);
+      const int a = static_cast<int>((kk >> kKeyIdxBits) & idx_mask);
+      if ((used >> a & 1u) || (used >> b & 1u)) {
+        ++overlap;
+        continue;
+      }
+      used |= (1u << a) | (1u << b);
+      const long long gain = kKeyGainMax - static_cast<long long>(kk >> (2 * kKeyIdxBits));
+      if (lane == 0) {
+        const int keep = q[a];
+        const int rem = q[b];
+        P.sel_keep[so + ns] = keep;
+        P.sel_rem[so + ns] = rem;
+        P.sel_gain[so + ns] = gain;
+        P.stamp[keep] = 2 * P.block_stamp;
+        P.stamp[rem] = 2 * P.block_stamp + 1;
+        P.partner[keep] = rem;
+        P.partner[rem] = keep;
+        P.seq[rem] = static_cast<int>(so + ns);
+        work += static_cast<unsigned long long>(P.qlen[keep] + P.qlen[rem]);
+      }
+      ++ns;
+      total += gain;
+    }
+    (void)g;
+    if (lane == 0) {
+      P.sel_cnt[ri] = ns;
+      atomicAdd(&acc[0], static_cast<unsigned long long>(nrej));
+      atomicAdd(&acc[1], static_cast<unsigned long long>(m));
+      atomicAdd(&acc[2], overlap);
+      atomicAdd(&acc[3], static_cast<unsigned long long>(m));
+      atomicAdd(&acc[4], static_cast<unsigned long long>(ns));
+      atomicAdd(&acc[5], static_cast<unsigned long long>(total));
+      atomicAdd(&acc[6], work);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (acc[0]) atomicAdd(&P.stats[kStRejThreshold], acc[0]);
+    if (acc[1]) atomicAdd(&P.stats[kStPositive], acc[1]);
+    if (acc[2]) atomicAdd(&P.stats[kStRejOverlap], acc[2]);
+    if (acc[3]) atomicAdd(&P.stats[kStCandPairs], acc[3]);
+    if (acc[4]) {
+      atomicAdd(&P.stats[kStSelected], acc[4]);
+      atomicAdd(&P.stats[kStValidationCalls], acc[4]);
+    }
+    if (acc[5]) {
+      atomicAdd(&P.stats[kStLocalGain], acc[5]);
+      atomicAdd(&P.stats[kStIsolatedGain], acc[5]);
+    }
+    if (acc[6]) atomicAdd(&P.stats[kStValidationWork], acc[6]);
   }
 }
 
@@ -1780,6 +1927,32 @@ void Engine::PrepareIterationBuffers() {
   }
   h_block_small_.push_back(static_cast<int>(h_small_.size()));
   h_block_big_.push_back(static_cast<int>(h_big_.size()));
+  // selection: groups of at most kSelectSmallGroup members (at most 28
+  // candidates) get one warp each, the others one CTA each
+  h_sel_small_.clear();
+  h_sel_big_.clear();
+  h_block_sel_small_.clear();
+  h_block_sel_big_.clear();
+  for (size_t b = 0; b + 1 < h_block_rg_.size(); ++b) {
+    h_block_sel_small_.push_back(static_cast<int>(h_sel_small_.size()));
+    h_block_sel_big_.push_back(static_cast<int>(h_sel_big_.size()));
+    for (int ri = h_block_rg_[b]; ri < h_block_rg_[b + 1]; ++ri) {
+      const int g = h_glen_[static_cast<size_t>(h_real_[static_cast<size_t>(ri)])];
+      (g <= kSelectSmallGroup ? h_sel_small_ : h_sel_big_).push_back(ri);
+    }
+  }
+  h_block_sel_small_.push_back(static_cast<int>(h_sel_small_.size()));
+  h_block_sel_big_.push_back(static_cast<int>(h_sel_big_.size()));
+  d_sel_small_.ensure(h_sel_small_.size() + 1);
+  d_sel_big_.ensure(h_sel_big_.size() + 1);
+  if (!h_sel_small_.empty()) {
+    CheckCuda(cudaMemcpyAsync(d_sel_small_.p, h_sel_small_.data(), sizeof(int) * h_sel_small_.size(),
+                              cudaMemcpyHostToDevice, stream_), "h2d select small list");
+  }
+  if (!h_sel_big_.empty()) {
+    CheckCuda(cudaMemcpyAsync(d_sel_big_.p, h_sel_big_.data(), sizeof(int) * h_sel_big_.size(),
+                              cudaMemcpyHostToDevice, stream_), "h2d select big list");
+  }
   d_small_.ensure(h_small_.size() + 1);
   d_big_.ensure(h_big_.size() + 1);
   d_bigdesc_.ensure(sizeof(BigDesc) * (h_big_.size() + 1));
@@ -1814,6 +1987,8 @@ void Engine::PrepareIterationBuffers() {
   d_sel_cnt_.ensure(R + 1);
   const size_t ncand = static_cast<size_t>(h_cand_off_[R]);
   d_cand_.ensure(ncand + 1);
+  d_cand_rep_.ensure(ncand + 1);
+  CheckCuda(cudaMemsetAsync(d_cand_rep_.p, 0xff, sizeof(int2) * (ncand + 1), stream_), "memset cand reps");
   d_res_.ensure(ncand + 1);
   if (cfg_.ranker) {
     d_cand_feat_.ensure(ncand + 1);
@@ -1911,6 +2086,7 @@ void Engine::LaunchPrepare(int s0, int s1, int b0, int b1) {
   PP.stats = d_stats_.p;
   PP.err = d_err_.p;
   PP.cand_feat = cfg_.ranker ? d_cand_feat_.p : nullptr;
+  PP.cand_rep = d_cand_rep_.p;
   BeginTimed(kTimePrepare);
   if (s1 > s0) {
     PP.list = d_small_.p;
@@ -1986,6 +2162,7 @@ void Engine::RunBlock(size_t b, double threshold, int iter, int total_iterations
   SP.cand_off = d_cand_off_.p;
   SP.cand = d_cand_.p;
   SP.cand_cnt = d_cand_cnt_.p;
+  SP.cand_rep = d_cand_rep_.p;
   SP.res = d_res_.p;
   SP.stats = d_stats_.p;
   SP.err = d_err_.p;
@@ -2048,8 +2225,23 @@ void Engine::RunBlock(size_t b, double threshold, int iter, int total_iterations
   LP.ctl = d_ctl_.p;
   LP.stats = d_stats_.p;
   LP.err = d_err_.p;
-  ++launches_;
-  SelectKernel<<<nrg, kSelectThreads, 8 * kSelectSmemKeys, stream_>>>(LP);
+  const int ss0 = h_block_sel_small_[b], ss1 = h_block_sel_small_[b + 1];
+  const int sb0 = h_block_sel_big_[b], sb1 = h_block_sel_big_[b + 1];
+  if (ss1 > ss0) {
+    LP.list = d_sel_small_.p;
+    LP.list0 = ss0;
+    LP.nlist = ss1 - ss0;
+    ++launches_;
+    SelectSmallKernel<<<(ss1 - ss0 + kSelectSmallWarps - 1) / kSelectSmallWarps, kSelectSmallWarps * 32, 0,
+                        stream_>>>(LP);
+  }
+  if (sb1 > sb0) {
+    LP.list = d_sel_big_.p;
+    LP.list0 = sb0;
+    LP.nlist = sb1 - sb0;
+    ++launches_;
+    SelectKernel<<<sb1 - sb0, kSelectThreads, 8 * kSelectSmemKeys, stream_>>>(LP);
+  }
   LaunchCommit(rg0, nrg, sel_slots, cfg_.verify_cuda_gain);
 }
 
