@@ -44,6 +44,10 @@ struct Options {
   bool ea_use_threshold = false;
   bool write_output = false;
   bool verify_cuda_gain = false;
+  bool ranker = false;
+  bool ranker_audit = false;
+  double ranker_recall = 0.99;
+  int ranker_train_iters = 5;
   bool show_help = false;
   double error_bound = 0.0;
   uint64_t seed = 1;
@@ -57,8 +61,10 @@ void PrintUsage() {
             << "--scoring-backend cuda --cost-objective mags-compatible --state-backend persistent\n"
             << "--quotient-update incremental --candidate-index legacy --certification off\n"
             << "--commit-policy g0 --threshold-policy reciprocal [--ea-use-threshold]\n"
+            << "(--merge-mode batch-ea: the same with one group per block)\n"
             << "Other options: --top-k --group-batch-size --iterations --print-offset --divide-hash-dims\n"
             << "--divide-max-group --seed --error-bound 0 --write-output --out <dir> --profiling --device\n"
+            << "--ranker [--ranker-recall r] [--ranker-train-iters k] [--ranker-audit]: learned candidate ranker\n"
             << "Input: text edge list 'u v' per line, or a binary edge list with a .bin suffix.\n";
 }
 
@@ -106,6 +112,10 @@ Options ParseArgs(int argc, char** argv) {
     else if (a == "--ea-use-threshold") o.ea_use_threshold = true;
     else if (a == "--write-output") o.write_output = true;
     else if (a == "--verify-cuda-gain") o.verify_cuda_gain = true;  // re-score and check every commit
+    else if (a == "--ranker") o.ranker = true;  // learned candidate ranker (this build's own)
+    else if (a == "--ranker-audit") o.ranker_audit = true;
+    else if (a == "--ranker-recall" && has) o.ranker_recall = std::stod(take());
+    else if (a == "--ranker-train-iters" && has) o.ranker_train_iters = std::stoi(take());
     else {
       std::cerr << "Unknown or incomplete argument: " << a << "\n";
       o.show_help = true;
@@ -130,7 +140,13 @@ int Run(int argc, char** argv) {
   }
   if (o.write_output && o.out_dir.empty()) throw std::runtime_error("--write-output requires --out <dir>.");
   Require("--scoring-backend", o.scoring_backend, "cuda");
-  Require("--merge-mode", o.merge_mode, "batch-ea-blocked");
+  // batch-ea (one group at a time, src/sweg.cpp:1147-1161) equals
+  // batch-ea-blocked with one group per block; --group-batch-size is then unused
+  if (o.merge_mode == "batch-ea") {
+    o.group_batch_size = 1;
+  } else {
+    Require("--merge-mode", o.merge_mode, "batch-ea-blocked");
+  }
   Require("--cost-objective", o.cost_objective, "mags-compatible");
   Require("--state-backend", o.state_backend, "persistent");
   Require("--quotient-update", o.quotient_update, "incremental");
@@ -181,6 +197,10 @@ int Run(int argc, char** argv) {
   cfg.seed = o.seed;
   cfg.device = o.device;
   cfg.verify_cuda_gain = o.verify_cuda_gain ? 1 : 0;
+  cfg.ranker = o.ranker ? 1 : 0;
+  cfg.ranker_audit = o.ranker_audit ? 1 : 0;
+  cfg.ranker_recall = static_cast<float>(o.ranker_recall);
+  cfg.ranker_train_iters = o.ranker_train_iters;
   beam_engine* e = nullptr;
   if (beam_engine_create(static_cast<int32_t>(n), arcs, beam_graph_row_ptr(g), beam_graph_col_idx(g), &cfg, &e) != 0) {
     throw std::runtime_error(beam_engine_last_error());
@@ -217,6 +237,8 @@ int Run(int argc, char** argv) {
   check(beam_engine_partition(e, labels.data(), head.data(), next.data()));
   beam_engine_stats st;
   check(beam_engine_get_stats(e, &st));
+  beam_ranker_info rk;
+  check(beam_engine_ranker_info(e, &rk));
   int64_t qnnz = 0;
   check(beam_engine_quotient_nnz(e, &qnnz));
   beam_engine_destroy(e);
@@ -316,6 +338,17 @@ int Run(int argc, char** argv) {
   Metric("candidate_proxy_pairs_examined", st.candidate_proxy_pairs_examined);
   Metric("exact_gain_input_nnz", st.exact_gain_input_nnz);
   Metric("merges_per_second", FormatDouble(run_ms > 0 ? 1000.0 * static_cast<double>(st.accepted_merges_after_validation) / run_ms : 0.0));
+  if (o.ranker) {
+    Metric("ranker_samples", rk.samples);
+    Metric("ranker_train_steps", rk.train_steps);
+    Metric("ranker_train_ms", FormatDouble(rk.train_ms));
+    Metric("ranker_ranked", rk.ranked);
+    Metric("ranker_pruned", rk.pruned);
+    if (o.ranker_audit) {
+      Metric("ranker_audit_passing", rk.audit_passing);
+      Metric("ranker_audit_lost", rk.audit_lost);
+    }
+  }
   beam_graph_free(g);
   return 0;
 }

@@ -24,9 +24,11 @@ def flag_value(flags, name, default):
 
 def options_from_flags(flags):
     """Engine/oracle keyword options for a list of reference flags."""
+    # --merge-mode batch-ea commits group by group: blocks of one group
+    batch_ea = flag_value(flags, "--merge-mode", "batch-ea-blocked") == "batch-ea"
     return {
         "top_k": int(flag_value(flags, "--top-k", 16)),
-        "group_batch_size": int(flag_value(flags, "--group-batch-size", 64)),
+        "group_batch_size": 1 if batch_ea else int(flag_value(flags, "--group-batch-size", 64)),
         "divide_hash_dims": int(flag_value(flags, "--divide-hash-dims", 16)),
         "divide_max_group": int(flag_value(flags, "--divide-max-group", 512)),
         "ea_use_threshold": "--ea-use-threshold" in flags,

@@ -118,6 +118,10 @@ CASES += [
      "flags": flags_with(seed=42, iterations=5)},
     {"name": "dcsbm_topk32_maxgroup1024", "spec": WORKLOADS["dcsbm_4096"],
      "flags": flags_with(top_k=32) + ["--divide-max-group", "1024"]},
+    # the non-blocked batch-ea mode (group by group)
+    {"name": "rmat12_batchea", "spec": "rmat:scale=12,ef=4,a=0.57,b=0.19,c=0.19,seed=3",
+     "flags": flags_with(merge_mode="batch-ea")},
+    {"name": "gnm_sparse_s2_batchea", "spec": "gnm:n=80,m=220,seed=2", "flags": flags_with(merge_mode="batch-ea")},
     {"name": "rmat19", "spec": WORKLOADS["rmat19"], "flags": flags_with(), "large": True},
 ]
 

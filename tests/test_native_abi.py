@@ -67,7 +67,7 @@ def test_cli_usage_and_missing_input(tmp_path):
 
 
 @pytest.mark.parametrize("flag,value", [("--scoring-backend", "cpu"), ("--cost-objective", "legacy"),
-                                        ("--merge-mode", "batch-ea"), ("--commit-policy", "t4"),
+                                        ("--merge-mode", "batch"), ("--commit-policy", "t4"),
                                         ("--certification", "safe"), ("--threshold-policy", "adaptive")])
 def test_cli_rejects_modes_outside_the_recommended_one(tmp_path, flag, value):
     from beam_gb300 import REFERENCE_FLAGS
