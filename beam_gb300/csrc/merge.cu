@@ -239,9 +239,11 @@ struct PrepareParams {
   DevError* err;
 };
 
-// Byte offset of the int64 old-cost array after a group's g*g tables
-// (8 + 8 + 4 + 1 bytes per member pair), rounded up to 8-byte alignment.
-__host__ __device__ __forceinline__ long long OldCostOffset(long long gg) { return (21 * gg + 7) & ~7ll; }
+// Per big group: proxy int64[g*g] | kept flag u8[g*g] | old cost int64[g];
+// the flag table starts at FlagOffset and the old costs at OldCostOffset
+// (rounded up to 8-byte alignment).
+__host__ __device__ __forceinline__ long long FlagOffset(long long gg) { return 8 * gg; }
+__host__ __device__ __forceinline__ long long OldCostOffset(long long gg) { return (9 * gg + 7) & ~7ll; }
 
 struct RankKey {
   double ratio;
@@ -345,7 +347,7 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
   const long long gg = static_cast<long long>(g) * g;
   unsigned char* mat = P.mat + P.mat_off[ri];
   long long* pmat = reinterpret_cast<long long*>(mat);
-  unsigned char* fmat = mat + 20 * gg;
+  unsigned char* fmat = mat + FlagOffset(gg);
   if (slots > 0) {
     // deferred group: row offsets and member scalars in block scratch, pair
     // tables zeroed, unused sort slots padded; fill / sort / accumulate follow
@@ -406,8 +408,7 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
   int* enx = S.enx;
   const unsigned hmask = kSmemHeads - 1;
   for (unsigned h = tid; h <= hmask; h += kPrepThreads) heads[h] = -1;
-  // per-group tables: proxy P int64[g*g] | ratio double[g*g] | partner
-  // int32[g*g] | kept flag u8[g*g] | old cost int64[g]
+  // per-group tables: proxy int64[g*g] | kept flag u8[g*g] | old cost int64[g]
   for (long long k = tid; k < gg; k += kPrepThreads) {
     pmat[k] = 0;
     fmat[k] = 0;
@@ -631,7 +632,7 @@ __global__ void __launch_bounds__(256) PrepareMembersKernel(PrepareParams P) {
   const long long gg = static_cast<long long>(g) * g;
   unsigned char* mat = P.mat + P.mat_off[ri];
   const long long* pmat = reinterpret_cast<const long long*>(mat);
-  unsigned char* fmat = mat + 20 * gg;
+  unsigned char* fmat = mat + FlagOffset(gg);
   const long long* old = reinterpret_cast<const long long*>(mat + OldCostOffset(gg));
   // per member: candidates with positive proxy, ratio, top-k (the ratio is
   // recomputed where it is needed instead of being stored)
@@ -775,7 +776,7 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareOutputKernel(PrepareParam
   const int gid = P.real[ri];
   const int g = P.glen[gid];
   const long long gg = static_cast<long long>(g) * g;
-  const unsigned char* fmat = P.mat + P.mat_off[ri] + 20 * gg;
+  const unsigned char* fmat = P.mat + P.mat_off[ri] + FlagOffset(gg);
   const long long* pmat = reinterpret_cast<const long long*>(P.mat + P.mat_off[ri]);
   const long long* old = reinterpret_cast<const long long*>(P.mat + P.mat_off[ri] + OldCostOffset(gg));
   const int* q = P.order + P.gstart[gid];
