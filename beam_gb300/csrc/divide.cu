@@ -23,6 +23,7 @@
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
+#include <cstring>
 #include <numeric>
 
 #include "engine.h"
@@ -65,6 +66,37 @@ __global__ void SegLenKernel(const int* __restrict__ seg_start, int segs, int co
     unf_flag[s] = unf;
     unf_len[s] = unf ? len : 0;
   }
+}
+
+// SegLenKernel over all count positions with the segment count read on the
+// device (no host round trip): entries past the last segment are zeroed, so
+// scans over count elements equal scans over the segments.
+__global__ void SegLenAllKernel(const int* __restrict__ seg_start, const int* __restrict__ segs_p, int count,
+                                int max_group, int* __restrict__ seg_len, int* __restrict__ unf_flag,
+                                int* __restrict__ unf_len) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= count) return;
+  const int segs = *segs_p;
+  if (s < segs) {
+    const int end = s + 1 < segs ? seg_start[s + 1] : count;
+    const int len = end - seg_start[s];
+    seg_len[s] = len;
+    const int unf = len > max_group ? 1 : 0;
+    unf_flag[s] = unf;
+    unf_len[s] = unf ? len : 0;
+  } else {
+    unf_flag[s] = 0;
+    unf_len[s] = 0;
+  }
+}
+
+// {segments, unfinished segments, their items} of a depth, for one read-back.
+__global__ void DepthCountsKernel(const int* __restrict__ incl_last, const int* __restrict__ unf_idx_last,
+                                  const int* __restrict__ unf_flag_last, const int* __restrict__ unf_off_last,
+                                  const int* __restrict__ unf_len_last, int* __restrict__ out) {
+  out[0] = *incl_last;
+  out[1] = *unf_idx_last + *unf_flag_last;
+  out[2] = *unf_off_last + *unf_len_last;
 }
 
 // Compact the items of unfinished segments: pos_map[k] = position,
@@ -214,7 +246,7 @@ void Engine::Divide(int iter) {
   const int T = 256;
   cudaStream_t s = stream_;
   // scratch arrays: d_counts_ holds [flags | scan | seg_len | unf_flag | unf_len | unf_idx | unf_off | ubeg | uend]
-  d_counts_.ensure(static_cast<size_t>(n) * 9 + 64);
+  d_counts_.ensure(static_cast<size_t>(n) * 9 + 64);  // + 3 depth counts after uend
   int* flags = d_counts_.p;
   int* scan = flags + n;
   int* seg_len = scan + n;
@@ -277,21 +309,24 @@ void Engine::Divide(int iter) {
       scan_incl(d_head_flag_.p, scan, count);
       ++launches_;
       SegStartsKernel<<<Blocks(count, T), T, 0, s>>>(d_head_flag_.p, scan, count, seg_start);
-      int seg_total = 0, dummy = 0;
-      fetch2(scan + count - 1, scan + count - 1, &seg_total, &dummy);
-      segs = seg_total;
       ++launches_;
-      SegLenKernel<<<Blocks(segs, T), T, 0, s>>>(seg_start, segs, count, cfg_.divide_max_group, seg_len, unf_flag,
-                                                 unf_len);
-      scan_excl(unf_flag, unf_idx, segs);
-      scan_excl(unf_len, unf_off, segs);
-      int nu_last = 0, nu_flag = 0;
-      fetch2(unf_idx + segs - 1, unf_flag + segs - 1, &nu_last, &nu_flag);
-      const int nu = nu_last + nu_flag;
+      SegLenAllKernel<<<Blocks(count, T), T, 0, s>>>(seg_start, scan + count - 1, count, cfg_.divide_max_group,
+                                                     seg_len, unf_flag, unf_len);
+      scan_excl(unf_flag, unf_idx, count);
+      scan_excl(unf_len, unf_off, count);
+      // one read-back per depth: segments, unfinished segments, their items
+      int* dc = uend + n;
+      ++launches_;
+      DepthCountsKernel<<<1, 1, 0, s>>>(scan + count - 1, unf_idx + count - 1, unf_flag + count - 1,
+                                        unf_off + count - 1, unf_len + count - 1, dc);
+      CheckCuda(cudaMemcpyAsync(h_pin_.p, dc, 3 * sizeof(int), cudaMemcpyDeviceToHost, s), "d2h depth counts");
+      CheckCuda(cudaStreamSynchronize(s), "sync");
+      int hc[3];
+      std::memcpy(hc, h_pin_.p, sizeof(hc));
+      segs = hc[0];
+      const int nu = hc[1];
       if (nu == 0) break;
-      int items_last = 0, items_len = 0;
-      fetch2(unf_off + segs - 1, unf_len + segs - 1, &items_last, &items_len);
-      const int items = items_last + items_len;
+      const int items = hc[2];
       ++launches_;
       CompactItemsKernel<<<Blocks(count, T), T, 0, s>>>(scan, seg_start, seg_len, unf_flag, unf_idx, unf_off, count,
                                                         d_pos_map_.p, item_seg, ubeg, uend);

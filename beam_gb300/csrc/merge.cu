@@ -38,7 +38,7 @@ constexpr int kSelectThreads = 512;
 constexpr int kSelectSmemKeys = 8192;
 constexpr int kRowsThreads = 256;
 constexpr int kRowSmem = 2048;       // staged row entries in shared memory
-constexpr int kClaimSmem = 4096;     // claimed neighbour rows listed in shared memory
+constexpr int kWarpRow = 32;         // neighbour rows rewritten by one warp
 constexpr int kKeyIdxBits = 10;      // a_idx, b_idx < kMaxGroup
 constexpr long long kKeyGainMax = (1ll << (64 - 2 * kKeyIdxBits)) - 1;
 
@@ -1563,6 +1563,8 @@ struct CommitParams {
   BlockCtl* ctl;
   unsigned long long* stats;
   DevError* err;
+  int* rows_short;  // claimed neighbour rows of at most kWarpRow entries (count: ctl->short_cnt)
+  int* rows_long;   // the other claimed neighbour rows (count: ctl->long_cnt)
 };
 
 // Optional re-validation (--verify-cuda-gain): recomputes the exact gain of
@@ -1602,7 +1604,6 @@ struct RowsSmem {
   Entry s[kRowSmem];
   int d[kRowSmem + 1];
   Entry ins[kRowSmem];
-  int claimed[kClaimSmem];
 };
 
 // Rewrites a staged sorted row S[0..L) (adjacent equal ids allowed: the keep
@@ -1723,8 +1724,7 @@ __global__ void __launch_bounds__(kRowsThreads) CommitKernel(CommitParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   RowsSmem& R = *reinterpret_cast<RowsSmem*>(smem_raw);
   __shared__ long long new_off;
-  __shared__ int nclaimed, folded_sum;
-  __shared__ int* claim_buf;
+  __shared__ int folded_sum;
   const QuotientView& Q = P.Q;
   const long long s0 = P.sel_off[P.rg0];
   const long long s1 = P.sel_off[P.rg0 + P.nrg];
@@ -1740,16 +1740,10 @@ __global__ void __launch_bounds__(kRowsThreads) CommitKernel(CommitParams P) {
     const int lr = Q.len[r];
     const int lk = Q.len[k];
     const int my_seq = static_cast<int>(slot);
-    if (tid == 0) {
-      nclaimed = 0;
-      folded_sum = 0;
-      claim_buf = lr <= kClaimSmem
-                      ? R.claimed
-                      : reinterpret_cast<int*>(ScratchAlloc(P.scratch, P.scratch_cap, P.ctl, 4ull * lr, P.err));
-    }
+    if (tid == 0) folded_sum = 0;
     __syncthreads();
-    if (claim_buf == nullptr) return;
-    // touched count and neighbour-row claims (block-start row of remove)
+    // touched count and neighbour-row claims (block-start row of remove); a
+    // claimed row goes to the short or long rewrite list
     int folded = 0;
     for (int i = tid; i < lr; i += kRowsThreads) {
       const int x = EntNb(rr[i]);
@@ -1757,12 +1751,17 @@ __global__ void __launch_bounds__(kRowsThreads) CommitKernel(CommitParams P) {
       const int sx = P.stamp[x];
       if (sx == remove_stamp && P.seq[x] < my_seq && RowLookup(rr, lr, P.partner[x]) != 0) ++folded;
       if ((sx >> 1) == P.block_stamp) continue;  // keep/remove rows are rebuilt by their own pair
-      if (atomicExch(&P.claim[x], P.block_stamp) != P.block_stamp) claim_buf[atomicAdd(&nclaimed, 1)] = x;
+      if (atomicExch(&P.claim[x], P.block_stamp) != P.block_stamp) {
+        if (Q.len[x] <= kWarpRow) {
+          P.rows_short[atomicAdd(&P.ctl->short_cnt, 1u)] = x;
+        } else {
+          P.rows_long[atomicAdd(&P.ctl->long_cnt, 1u)] = x;
+        }
+      }
     }
     folded = WarpSumInt(folded);
     if ((tid & 31) == 0 && folded) atomicAdd(&folded_sum, folded);
     __syncthreads();
-    const int claimed = nclaimed;
     // keep row <- merge(row k, row r), staged with keep entries first on ties
     const int L = lk + lr;
     Entry *S, *INS;
@@ -1814,27 +1813,98 @@ __global__ void __launch_bounds__(kRowsThreads) CommitKernel(CommitParams P) {
                 static_cast<unsigned long long>(2 + 3 * (lr - (ekr > 0 ? 1 : 0) - folded_sum)));
       atomicAdd(&P.stats[kStUpdateBytes], 8ull * (2ull * L + nl));
     }
-    // neighbour rows claimed by this pair, rewritten in place
-    for (int c = 0; c < claimed; ++c) {
-      const int x = claim_buf[c];
-      Entry* rowp = Q.ent + Q.off[x];
-      const int lx = Q.len[x];
-      Entry *S2, *INS2;
-      int* D2;
-      if (!StageBuffers(P, R, lx, &S2, &D2, &INS2)) return;
-      for (int i = tid; i < lx; i += kRowsThreads) S2[i] = rowp[i];
-      __syncthreads();
-      const int nlx = RewriteRow(P, S2, lx, D2, INS2, -1, -1, rowp);
-      if (tid == 0) {
-        Q.len[x] = nlx;
-        atomicAdd(&P.stats[kStRowsRewritten], 1ull);
-        atomicAdd(&P.stats[kStRowEntriesRewritten], static_cast<unsigned long long>(lx));
-        atomicAdd(&P.stats[kStUpdateBytes], 8ull * (lx + nlx));
+    __syncthreads();
+  }
+}
+
+// Claimed neighbour rows of at most kWarpRow entries, one warp per row: each
+// entry of a supernode removed in this block is renamed to its keep partner,
+// the row is sorted by neighbour (register bitonic sort), equal neighbours
+// are summed and the row is compacted in place (it can only shrink).
+__device__ void RewriteShortRows(const CommitParams& P) {
+  const QuotientView& Q = P.Q;
+  const int lane = threadIdx.x & 31;
+  const unsigned cnt = P.ctl->short_cnt;
+  const int remove_stamp = 2 * P.block_stamp + 1;
+  const long long nw = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
+  unsigned long long rows = 0, entries = 0, bytes = 0;
+  for (long long idx = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; idx < cnt; idx += nw) {
+    const int x = P.rows_short[idx];
+    Entry* row = Q.ent + Q.off[x];
+    const int lx = Q.len[x];
+    unsigned long long key = ~0ull;
+    if (lane < lx) {
+      const Entry e = row[lane];
+      int id = EntNb(e);
+      if (P.stamp[id] == remove_stamp) id = P.partner[id];
+      key = static_cast<unsigned long long>(id) << 32 | static_cast<unsigned long long>(EntCnt(e));
+    }
+    key = WarpBitonicSortAsc(key, lane);
+    const bool valid = key != ~0ull;
+    const int id = static_cast<int>(key >> 32);
+    const long long c = valid ? static_cast<long long>(key & 0xffffffffull) : 0;
+    const int prev = __shfl_up_sync(0xffffffffu, id, 1);
+    const bool head = valid && (lane == 0 || prev != id);
+    long long total = c;
+    bool more = head;
+    for (int j = 1; j < 32; ++j) {
+      const int idj = __shfl_down_sync(0xffffffffu, id, j);
+      const long long cj = __shfl_down_sync(0xffffffffu, c, j);
+      if (more && lane + j < 32 && idj == id) {
+        total += cj;
+      } else {
+        more = false;
       }
-      __syncthreads();
+      if (!__any_sync(0xffffffffu, more)) break;
+    }
+    const unsigned heads = __ballot_sync(0xffffffffu, head);
+    if (head) row[__popc(heads & ((1u << lane) - 1u))] = MakeEnt(id, total);
+    const int nl = __popc(heads);
+    if (lane == 0) {
+      Q.len[x] = nl;
+      ++rows;
+      entries += static_cast<unsigned long long>(lx);
+      bytes += 8ull * static_cast<unsigned long long>(lx + nl);
+    }
+  }
+  if (lane == 0 && rows) {
+    atomicAdd(&P.stats[kStRowsRewritten], rows);
+    atomicAdd(&P.stats[kStRowEntriesRewritten], entries);
+    atomicAdd(&P.stats[kStUpdateBytes], bytes);
+  }
+}
+
+// Claimed neighbour rows longer than kWarpRow entries, one CTA per row.
+__device__ void RewriteLongRows(const CommitParams& P, RowsSmem& R) {
+  const QuotientView& Q = P.Q;
+  const unsigned cnt = P.ctl->long_cnt;
+  for (unsigned idx = blockIdx.x; idx < cnt; idx += gridDim.x) {
+    const int x = P.rows_long[idx];
+    Entry* rowp = Q.ent + Q.off[x];
+    const int lx = Q.len[x];
+    Entry *S2, *INS2;
+    int* D2;
+    if (!StageBuffers(P, R, lx, &S2, &D2, &INS2)) return;
+    for (int i = threadIdx.x; i < lx; i += kRowsThreads) S2[i] = rowp[i];
+    __syncthreads();
+    const int nlx = RewriteRow(P, S2, lx, D2, INS2, -1, -1, rowp);
+    if (threadIdx.x == 0) {
+      Q.len[x] = nlx;
+      atomicAdd(&P.stats[kStRowsRewritten], 1ull);
+      atomicAdd(&P.stats[kStRowEntriesRewritten], static_cast<unsigned long long>(lx));
+      atomicAdd(&P.stats[kStUpdateBytes], 8ull * (lx + nlx));
     }
     __syncthreads();
   }
+}
+
+// All claimed neighbour rows of a block: the long ones by whole CTAs first,
+// then the short ones by single warps.
+__global__ void __launch_bounds__(kRowsThreads) RewriteRowsKernel(CommitParams P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  RowsSmem& R = *reinterpret_cast<RowsSmem*>(smem_raw);
+  RewriteLongRows(P, R);
+  RewriteShortRows(P);
 }
 
 __global__ void ScatterGroupKernel(const int* __restrict__ q, const int* __restrict__ idx, int g,
@@ -1864,6 +1934,8 @@ void Engine::ConfigureKernels() {
                                  8 * kSelectSmemKeys), "select smem attribute");
   CheckCuda(cudaFuncSetAttribute(CommitKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(sizeof(RowsSmem))), "commit smem attribute");
+  CheckCuda(cudaFuncSetAttribute(RewriteRowsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(sizeof(RowsSmem))), "rewrite smem attribute");
 }
 
 // Per-iteration layout: the groups with >= 2 members in Divide order, their
@@ -2052,6 +2124,8 @@ void Engine::LaunchCommit(int rg0, int nrg, int64_t max_pairs, bool verify) {
   C.ctl = d_ctl_.p;
   C.stats = d_stats_.p;
   C.err = d_err_.p;
+  C.rows_short = d_rows_short_.p;
+  C.rows_long = d_rows_long_.p;
   if (verify) {
     const int vb = static_cast<int>(std::min<int64_t>((max_pairs + 7) / 8 + 1, 152 * 8));
     ++launches_;
@@ -2061,6 +2135,8 @@ void Engine::LaunchCommit(int rg0, int nrg, int64_t max_pairs, bool verify) {
   BeginTimed(kTimeUpdate);
   ++launches_;
   CommitKernel<<<grid, kRowsThreads, sizeof(RowsSmem), stream_>>>(C);
+  ++launches_;
+  RewriteRowsKernel<<<kRowsGrid, kRowsThreads, sizeof(RowsSmem), stream_>>>(C);
   EndTimed(kTimeUpdate);
 }
 
