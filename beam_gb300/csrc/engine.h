@@ -242,9 +242,9 @@ class Engine {
   std::vector<int> h_small_, h_big_;              // real-group positions by prepare kernel
   std::vector<int> h_block_small_, h_block_big_;  // per block: first entry in those lists
   DevBuf<int> d_small_, d_big_;
-  std::vector<int> h_sel_small_, h_sel_big_;              // real-group positions by select kernel
-  std::vector<int> h_block_sel_small_, h_block_sel_big_;  // per block: first entry in those lists
-  DevBuf<int> d_sel_small_, d_sel_big_;
+  std::vector<int> h_sel_small_, h_sel_mid_, h_sel_big_;  // real-group positions by select kernel
+  std::vector<int> h_block_sel_small_, h_block_sel_mid_, h_block_sel_big_;  // per block: first entries
+  DevBuf<int> d_sel_small_, d_sel_mid_, d_sel_big_;
   DevBuf<unsigned char> d_bigdesc_;  // per big-group entry: deferred-group descriptor
   std::vector<long long> h_soff_;    // sort-slot prefix over h_big_ (deferred groups)
   DevBuf<long long> d_soff_;

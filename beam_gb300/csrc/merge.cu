@@ -36,6 +36,9 @@ constexpr int kSmemHeads = 4096;     // bucket hash heads in shared memory
 constexpr int kScoreThreads = 256;
 constexpr int kSelectThreads = 512;
 constexpr int kSelectSmemKeys = 8192;
+constexpr int kSelectMidGroup = 32;   // groups of 9..32 members: a small CTA each
+constexpr int kSelectMidThreads = 128;
+constexpr int kSelectMidKeys = 512;   // >= min(C(32,2), 16 * 32) candidates
 constexpr int kRowsThreads = 256;
 constexpr int kRowSmem = 2048;       // staged row entries in shared memory
 constexpr int kWarpRow = 32;         // neighbour rows rewritten by one warp
@@ -1296,7 +1299,8 @@ __device__ void CtaBitonicSort(unsigned long long* keys, int n) {
 // block-start state its score came from (gain > 0 by the filter), so every
 // one is accepted; their endpoints are marked here (stamp, partner, commit
 // order) for the commit kernel.
-__global__ void __launch_bounds__(kSelectThreads) SelectKernel(SelectParams P) {
+template <int kThreads, int kSmemKeys>
+__global__ void __launch_bounds__(kThreads) SelectKernel(SelectParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned long long* skeys = reinterpret_cast<unsigned long long*>(smem_raw);
   __shared__ unsigned char used[kMaxGroup];
@@ -1318,10 +1322,10 @@ __global__ void __launch_bounds__(kSelectThreads) SelectKernel(SelectParams P) {
     nkeys = 0;
     rej_thr = 0;
     positive = 0;
-    gkeys = cap <= kSelectSmemKeys ? skeys
+    gkeys = cap <= kSmemKeys ? skeys
                                    : ScratchAlloc(P.scratch, P.scratch_cap, P.ctl, 8ull * cap, P.err);
   }
-  for (int i = tid; i < g; i += kSelectThreads) used[i] = 0;
+  for (int i = tid; i < g; i += kThreads) used[i] = 0;
   __syncthreads();
   unsigned long long* keys = gkeys;
   if (keys == nullptr) {
@@ -1330,7 +1334,7 @@ __global__ void __launch_bounds__(kSelectThreads) SelectKernel(SelectParams P) {
   }
   const long long base = P.cand_off[ri];
   unsigned long long my_rej = 0, my_pos = 0;
-  for (int c = tid; c < cnt; c += kSelectThreads) {
+  for (int c = tid; c < cnt; c += kThreads) {
     const longlong2 r = P.res[base + c];
     const long long gain = r.x;
     const long long before = r.y;
@@ -1364,7 +1368,7 @@ __global__ void __launch_bounds__(kSelectThreads) SelectKernel(SelectParams P) {
   const int m = nkeys;
   int pow2 = 1;
   while (pow2 < m) pow2 <<= 1;
-  for (int i = m + tid; i < pow2; i += kSelectThreads) keys[i] = ~0ull;
+  for (int i = m + tid; i < pow2; i += kThreads) keys[i] = ~0ull;
   __syncthreads();
   if (m > 1) CtaBitonicSort(keys, pow2);
   if (tid == 0) {
@@ -1411,6 +1415,170 @@ __global__ void __launch_bounds__(kSelectThreads) SelectKernel(SelectParams P) {
     atomicAdd(&P.stats[kStValidationCalls], static_cast<unsigned long long>(ns));
     atomicAdd(&P.stats[kStValidationWork], work);
     atomicAdd(&P.stats[kStIsolatedGain], static_cast<unsigned long long>(total));
+  }
+}
+
+// Groups of more than kSelectMidGroup members: the g0 greedy pass over keys
+// in ascending order selects exactly the edges that are, in some round of
+// the following loop, the smallest live key at both of their endpoints
+// (keys are distinct): per round every live key bids for its two endpoints
+// (shared-memory atomicMin), keys that win both are selected, keys touching
+// a selected endpoint die. Only the selected keys (at most g/2) are then
+// sorted, which gives the greedy order of the commit list; a key is skipped
+// by the greedy pass exactly when it is not selected, so the overlap count
+// is the number of keys minus the selected ones.
+constexpr int kMatchThreads = 512;
+constexpr int kMatchSmemKeys = 8192;
+
+__global__ void __launch_bounds__(kMatchThreads) SelectMatchKernel(SelectParams P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned long long* skeys = reinterpret_cast<unsigned long long*>(smem_raw);
+  __shared__ unsigned long long best[kMaxGroup];
+  __shared__ unsigned long long chosen[kMaxGroup / 2];
+  __shared__ unsigned char matched[kMaxGroup];
+  __shared__ int nkeys, nchosen, live_any;
+  __shared__ unsigned long long* gkeys;
+  __shared__ unsigned long long rej_thr;
+  const int tid = threadIdx.x;
+  const int ri = P.list[P.list0 + blockIdx.x];
+  const int gid = P.real[ri];
+  const int g = P.glen[gid];
+  const int cnt = g >= 2 && g <= kMaxGroup ? P.cand_cnt[ri] : 0;
+  if (cnt == 0) {
+    if (tid == 0) P.sel_cnt[ri] = 0;
+    return;
+  }
+  if (tid == 0) {
+    nkeys = 0;
+    nchosen = 0;
+    rej_thr = 0;
+    gkeys = cnt <= kMatchSmemKeys ? skeys
+                                  : ScratchAlloc(P.scratch, P.scratch_cap, P.ctl, 8ull * cnt, P.err);
+  }
+  for (int i = tid; i < g; i += kMatchThreads) matched[i] = 0;
+  __syncthreads();
+  unsigned long long* keys = gkeys;
+  if (keys == nullptr) {
+    if (tid == 0) P.sel_cnt[ri] = 0;
+    return;
+  }
+  const long long base = P.cand_off[ri];
+  unsigned long long my_rej = 0;
+  for (int c = tid; c < cnt; c += kMatchThreads) {
+    const longlong2 r = P.res[base + c];
+    const long long gain = r.x;
+    const long long before = r.y;
+    if (before < 0) continue;  // pruned by the ranker before scoring
+    bool ok = gain > 0;
+    if (ok && P.use_threshold) {
+      ok = before > 0 && static_cast<double>(gain) / static_cast<double>(before) >= P.threshold;
+    }
+    if (!ok) {
+      ++my_rej;
+      continue;
+    }
+    if (gain > kKeyGainMax) RaiseError(P.err, kErrKeyRange, gid, c, 0);
+    const int2 ab = P.cand[base + c];
+    keys[atomicAdd(&nkeys, 1)] = (static_cast<unsigned long long>(kKeyGainMax - gain) << (2 * kKeyIdxBits)) |
+                                 (static_cast<unsigned long long>(ab.x) << kKeyIdxBits) |
+                                 static_cast<unsigned long long>(ab.y);
+  }
+  if (my_rej) atomicAdd(&rej_thr, my_rej);
+  __syncthreads();
+  const int m = nkeys;
+  const unsigned long long idx_mask = (1ull << kKeyIdxBits) - 1;
+  // rounds of locally dominant keys (each round selects at least the
+  // smallest live key, so at most g/2 rounds)
+  for (int round = 0; round <= kMaxGroup / 2; ++round) {
+    for (int i = tid; i < g; i += kMatchThreads) best[i] = ~0ull;
+    if (tid == 0) live_any = 0;
+    __syncthreads();
+    for (int k = tid; k < m; k += kMatchThreads) {
+      const unsigned long long key = keys[k];
+      if (key == ~0ull) continue;
+      atomicMin(&best[(key >> kKeyIdxBits) & idx_mask], key);
+      atomicMin(&best[key & idx_mask], key);
+    }
+    __syncthreads();
+    for (int k = tid; k < m; k += kMatchThreads) {
+      const unsigned long long key = keys[k];
+      if (key == ~0ull) continue;
+      const int a = static_cast<int>((key >> kKeyIdxBits) & idx_mask);
+      const int b = static_cast<int>(key & idx_mask);
+      if (best[a] == key && best[b] == key) {
+        matched[a] = 1;
+        matched[b] = 1;
+        chosen[atomicAdd(&nchosen, 1)] = key;
+      }
+    }
+    __syncthreads();
+    for (int k = tid; k < m; k += kMatchThreads) {
+      const unsigned long long key = keys[k];
+      if (key == ~0ull) continue;
+      if (matched[(key >> kKeyIdxBits) & idx_mask] || matched[key & idx_mask]) {
+        keys[k] = ~0ull;
+      } else {
+        live_any = 1;
+      }
+    }
+    __syncthreads();
+    if (!live_any) break;
+  }
+  // the selected keys in greedy (ascending key) order
+  const int ns = nchosen;
+  int pow2 = 1;
+  while (pow2 < ns) pow2 <<= 1;
+  for (int i = ns + tid; i < pow2; i += kMatchThreads) chosen[i] = ~0ull;
+  __syncthreads();
+  if (ns > 1) CtaBitonicSort(chosen, pow2);
+  const int* q = P.order + P.gstart[gid];
+  const long long so = P.sel_off[ri];
+  long long my_total = 0;
+  unsigned long long my_work = 0;
+  for (int i = tid; i < ns; i += kMatchThreads) {
+    const unsigned long long key = chosen[i];
+    const int a = static_cast<int>((key >> kKeyIdxBits) & idx_mask);
+    const int b = static_cast<int>(key & idx_mask);
+    const long long gain = kKeyGainMax - static_cast<long long>(key >> (2 * kKeyIdxBits));
+    const int keep = q[a];
+    const int rem = q[b];
+    P.sel_keep[so + i] = keep;
+    P.sel_rem[so + i] = rem;
+    P.sel_gain[so + i] = gain;
+    P.stamp[keep] = 2 * P.block_stamp;
+    P.stamp[rem] = 2 * P.block_stamp + 1;
+    P.partner[keep] = rem;
+    P.partner[rem] = keep;
+    P.seq[rem] = static_cast<int>(so + i);
+    my_work += static_cast<unsigned long long>(P.qlen[keep] + P.qlen[rem]);
+    my_total += gain;
+  }
+  // chosen[] is no longer needed: reuse best[] for the two sums
+  __syncthreads();
+  if (tid == 0) {
+    best[0] = 0;
+    best[1] = 0;
+  }
+  __syncthreads();
+  my_total = WarpSum(my_total);
+  my_work = static_cast<unsigned long long>(WarpSum(static_cast<long long>(my_work)));
+  if ((tid & 31) == 0) {
+    if (my_total) atomicAdd(&best[0], static_cast<unsigned long long>(my_total));
+    if (my_work) atomicAdd(&best[1], my_work);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const unsigned long long total = best[0];
+    P.sel_cnt[ri] = ns;
+    atomicAdd(&P.stats[kStRejThreshold], rej_thr);
+    atomicAdd(&P.stats[kStPositive], static_cast<unsigned long long>(m));
+    atomicAdd(&P.stats[kStRejOverlap], static_cast<unsigned long long>(m - ns));
+    atomicAdd(&P.stats[kStCandPairs], static_cast<unsigned long long>(m));
+    atomicAdd(&P.stats[kStSelected], static_cast<unsigned long long>(ns));
+    atomicAdd(&P.stats[kStLocalGain], total);
+    atomicAdd(&P.stats[kStValidationCalls], static_cast<unsigned long long>(ns));
+    atomicAdd(&P.stats[kStValidationWork], best[1]);
+    atomicAdd(&P.stats[kStIsolatedGain], total);
   }
 }
 
@@ -1930,8 +2098,8 @@ void Engine::ConfigureKernels() {
                                  static_cast<int>(sizeof(PrepSmem))), "prepare smem attribute");
   CheckCuda(cudaFuncSetAttribute(PrepareSmallKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(sizeof(SmallSmem))), "prepare-small smem attribute");
-  CheckCuda(cudaFuncSetAttribute(SelectKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 8 * kSelectSmemKeys), "select smem attribute");
+  CheckCuda(cudaFuncSetAttribute(SelectMatchKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 8 * kMatchSmemKeys), "select smem attribute");
   CheckCuda(cudaFuncSetAttribute(CommitKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(sizeof(RowsSmem))), "commit smem attribute");
   CheckCuda(cudaFuncSetAttribute(RewriteRowsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2003,21 +2171,30 @@ void Engine::PrepareIterationBuffers() {
   // selection: groups of at most kSelectSmallGroup members (at most 28
   // candidates) get one warp each, the others one CTA each
   h_sel_small_.clear();
+  h_sel_mid_.clear();
   h_sel_big_.clear();
   h_block_sel_small_.clear();
+  h_block_sel_mid_.clear();
   h_block_sel_big_.clear();
   for (size_t b = 0; b + 1 < h_block_rg_.size(); ++b) {
     h_block_sel_small_.push_back(static_cast<int>(h_sel_small_.size()));
+    h_block_sel_mid_.push_back(static_cast<int>(h_sel_mid_.size()));
     h_block_sel_big_.push_back(static_cast<int>(h_sel_big_.size()));
     for (int ri = h_block_rg_[b]; ri < h_block_rg_[b + 1]; ++ri) {
       const int g = h_glen_[static_cast<size_t>(h_real_[static_cast<size_t>(ri)])];
-      (g <= kSelectSmallGroup ? h_sel_small_ : h_sel_big_).push_back(ri);
+      (g <= kSelectSmallGroup ? h_sel_small_ : g <= kSelectMidGroup ? h_sel_mid_ : h_sel_big_).push_back(ri);
     }
   }
   h_block_sel_small_.push_back(static_cast<int>(h_sel_small_.size()));
+  h_block_sel_mid_.push_back(static_cast<int>(h_sel_mid_.size()));
   h_block_sel_big_.push_back(static_cast<int>(h_sel_big_.size()));
   d_sel_small_.ensure(h_sel_small_.size() + 1);
+  d_sel_mid_.ensure(h_sel_mid_.size() + 1);
   d_sel_big_.ensure(h_sel_big_.size() + 1);
+  if (!h_sel_mid_.empty()) {
+    CheckCuda(cudaMemcpyAsync(d_sel_mid_.p, h_sel_mid_.data(), sizeof(int) * h_sel_mid_.size(),
+                              cudaMemcpyHostToDevice, stream_), "h2d select mid list");
+  }
   if (!h_sel_small_.empty()) {
     CheckCuda(cudaMemcpyAsync(d_sel_small_.p, h_sel_small_.data(), sizeof(int) * h_sel_small_.size(),
                               cudaMemcpyHostToDevice, stream_), "h2d select small list");
@@ -2312,12 +2489,20 @@ void Engine::RunBlock(size_t b, double threshold, int iter, int total_iterations
     SelectSmallKernel<<<(ss1 - ss0 + kSelectSmallWarps - 1) / kSelectSmallWarps, kSelectSmallWarps * 32, 0,
                         stream_>>>(LP);
   }
+  const int sm0 = h_block_sel_mid_[b], sm1 = h_block_sel_mid_[b + 1];
+  if (sm1 > sm0) {
+    LP.list = d_sel_mid_.p;
+    LP.list0 = sm0;
+    LP.nlist = sm1 - sm0;
+    ++launches_;
+    SelectKernel<kSelectMidThreads, kSelectMidKeys><<<sm1 - sm0, kSelectMidThreads, 8 * kSelectMidKeys, stream_>>>(LP);
+  }
   if (sb1 > sb0) {
     LP.list = d_sel_big_.p;
     LP.list0 = sb0;
     LP.nlist = sb1 - sb0;
     ++launches_;
-    SelectKernel<<<sb1 - sb0, kSelectThreads, 8 * kSelectSmemKeys, stream_>>>(LP);
+    SelectMatchKernel<<<sb1 - sb0, kMatchThreads, 8 * kMatchSmemKeys, stream_>>>(LP);
   }
   LaunchCommit(rg0, nrg, sel_slots, cfg_.verify_cuda_gain);
 }
