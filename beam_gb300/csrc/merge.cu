@@ -863,6 +863,7 @@ struct SmallWarpSmem {
   int len[kSmallGroup];
   int start[kSmallGroup + 1];
   unsigned fmask[kSmallGroup];
+  long long off[kSmallGroup];
 };
 
 struct SmallSmem {
@@ -891,6 +892,7 @@ __global__ void __launch_bounds__(kSmallWarps * 32) PrepareSmallKernel(PreparePa
     len = Q.len[rep];
     off = Q.off[rep];
     S.len[lane] = len;
+    S.off[lane] = off;
     S.fmask[lane] = 0;
   }
   // row starts in the staging buffer
@@ -905,17 +907,22 @@ __global__ void __launch_bounds__(kSmallWarps * 32) PrepareSmallKernel(PreparePa
   const int npairs = g * (g - 1) / 2;
   for (int k = lane; k < npairs; k += 32) S.p[k] = 0;
   const bool staged = E <= kSmallStage;
+  __syncwarp();
   if (staged) {
-    for (int i = 0; i < g; ++i) {
-      const long long oi = __shfl_sync(0xffffffffu, off, i);
-      const int li2 = __shfl_sync(0xffffffffu, len, i);
-      const int si = __shfl_sync(0xffffffffu, incl - len, i);
-      for (int k = lane; k < li2; k += 32) {
-        const Entry e = Q.ent[oi + k];
-        S.ent[si + k] = e;
-        S.tsz[si + k] = Q.size[EntNb(e)];
+    // one flat pass over the group's entries (independent loads), then the
+    // target sizes
+#pragma unroll 4
+    for (int k = lane; k < E; k += 32) {
+      int lo = 0, hi = g;  // row of entry k: last i with start[i] <= k
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (S.start[mid] <= k) lo = mid; else hi = mid;
       }
+      S.ent[k] = Q.ent[S.off[lo] + (k - S.start[lo])];
     }
+    __syncwarp();
+#pragma unroll 4
+    for (int k = lane; k < E; k += 32) S.tsz[k] = Q.size[EntNb(S.ent[k])];
   }
   __syncwarp();
   unsigned long long examined = 0;
@@ -1034,7 +1041,13 @@ __global__ void __launch_bounds__(kSmallWarps * 32) PrepareSmallKernel(PreparePa
   // per member (one lane each): positive partners, ratio, top-k
   int top_k = P.top_k < g - 1 ? P.top_k : g - 1;
   if (top_k < 1) top_k = 1;
-  if (lane < g) {
+  if (lane < g && g - 1 <= P.top_k) {
+    // every member has at most top_k partners: all positive ones are kept
+    const int i = lane;
+    for (int j = i + 1; j < g; ++j) {
+      if (S.p[TriIndex(i, j, g)] > 0) atomicOr(&S.fmask[i], 1u << j);
+    }
+  } else if (lane < g) {
     const int i = lane;
     const int qi = S.q[i];
     RankKey lst[kLaneTopK];
@@ -2214,6 +2227,13 @@ void Engine::PrepareIterationBuffers() {
   for (int k = 0; k < 2; ++k) {
     d_skey_[k].ensure(static_cast<size_t>(max_slots));
     d_sval_[k].ensure(static_cast<size_t>(max_slots));
+  }
+  // radix-sort scratch of the deferred groups, sized once per iteration
+  if (max_slots > 1) {
+    size_t bytes = 0;
+    CheckCuda(cub::DeviceRadixSort::SortPairs(nullptr, bytes, d_skey_[0].p, d_skey_[1].p, d_sval_[0].p,
+                                              d_sval_[1].p, max_slots, 0, 64, stream_), "cub radix sort size");
+    d_cub_tmp_.ensure(bytes);
   }
   d_soff_.ensure(h_soff_.size());
   CheckCuda(cudaMemcpyAsync(d_soff_.p, h_soff_.data(), sizeof(long long) * h_soff_.size(), cudaMemcpyHostToDevice,

@@ -40,8 +40,9 @@ def iterations_from_flags(flags):
     return int(flag_value(flags, "--iterations", 20))
 
 
-def golden_cases(include_large=True):
-    return [c for c in GOLDEN["cases"] if include_large or not c["large"]]
+def golden_cases(include_large=True, include_huge=True):
+    return [c for c in GOLDEN["cases"]
+            if (include_large or not c["large"]) and (include_huge or not c.get("huge", False))]
 
 
 def graph_for(case):

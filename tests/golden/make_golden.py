@@ -123,6 +123,11 @@ CASES += [
      "flags": flags_with(merge_mode="batch-ea")},
     {"name": "gnm_sparse_s2_batchea", "spec": "gnm:n=80,m=220,seed=2", "flags": flags_with(merge_mode="batch-ea")},
     {"name": "rmat19", "spec": WORKLOADS["rmat19"], "flags": flags_with(), "large": True},
+    # the batched form: one block holding every group of an iteration
+    {"name": "rmat19_batched", "spec": WORKLOADS["rmat19"], "flags": flags_with(group_batch_size=1 << 30),
+     "large": True},
+    {"name": "union_batched", "spec": WORKLOADS["grid_chunglu_union"], "flags": flags_with(group_batch_size=1 << 30),
+     "large": True, "huge": True},
 ]
 
 
@@ -181,6 +186,7 @@ def main() -> None:
         else:
             entry["edges"] = case["edges"]
         entry["large"] = bool(case.get("large"))
+        entry["huge"] = bool(case.get("huge"))  # too slow for the CPU oracle in the CPU suite
         entry["graph_sha256"] = graph_checksum(text)
         entry["metrics"] = metrics
         entry["files_sha256"] = hashes

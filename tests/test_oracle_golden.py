@@ -30,7 +30,7 @@ def oracle_metrics(o, enc):
     return {k: str(v) for k, v in m.items()}
 
 
-@pytest.mark.parametrize("case", golden_cases(), ids=lambda c: c["name"])
+@pytest.mark.parametrize("case", golden_cases(include_huge=False), ids=lambda c: c["name"])
 def test_oracle_matches_reference(case, tmp_path):
     g = graph_for(case)
     o = Oracle.from_graph(g, **options_from_flags(case["flags"]))
