@@ -241,6 +241,9 @@ int Run(int argc, char** argv) {
   check(beam_engine_ranker_info(e, &rk));
   int64_t qnnz = 0;
   check(beam_engine_quotient_nnz(e, &qnnz));
+  // CostOracle::ExactPartitionCost on the device (src/main.cpp:560)
+  int64_t exact = 0;
+  check(beam_engine_exact_partition_cost(e, &exact));
   beam_engine_destroy(e);
 
   const auto enc0 = Clock::now();
@@ -251,11 +254,6 @@ int Run(int argc, char** argv) {
     throw std::runtime_error(beam_encode_last_error());
   }
   const double encode_ms = std::chrono::duration<double, std::milli>(Clock::now() - enc0).count();
-  int64_t exact = 0;
-  if (beam_exact_partition_cost(static_cast<int32_t>(n), beam_graph_row_ptr(g), beam_graph_col_idx(g), labels.data(),
-                                &exact) != 0) {
-    throw std::runtime_error(beam_encode_last_error());
-  }
   if (enc.encoding_cost_standard != exact) {
     throw std::runtime_error("MAGS-compatible payload cost differs from exact partition cost");
   }

@@ -673,6 +673,10 @@ int beam_engine_ranker_info(beam_engine* e, beam_ranker_info* out) {
   });
 }
 
+int beam_engine_exact_partition_cost(beam_engine* e, int64_t* cost) {
+  return Guard([&] { *cost = e->impl->ExactPartitionCost(); });
+}
+
 int beam_engine_quotient_nnz(beam_engine* e, int64_t* nnz) {
   return Guard([&] { *nnz = e->impl->QuotientNnz(); });
 }

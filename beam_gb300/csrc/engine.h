@@ -139,6 +139,8 @@ class Engine {
   int64_t ExportRow(int rep, int32_t* nb, int64_t* cnt, int64_t cap, int64_t* size, int64_t* internal);
   void DeviceStats(uint64_t* out, int count);
   int64_t QuotientNnz();
+  // CostOracle::ExactPartitionCost of the current partition, from the input graph.
+  int64_t ExactPartitionCost();
   const HostStats& host_stats() const { return hstats_; }
   const RankerInfo& ranker_info() const { return rk_info_; }
   int64_t active_count() const { return n_active_; }
@@ -258,6 +260,10 @@ class Engine {
   int64_t n_active_ = 0;
   int64_t n_groups_ = 0;
   HostStats hstats_;
+
+  // exact partition cost
+  DevBuf<unsigned long long> d_pc_keys_[2], d_pc_scalars_;
+  DevBuf<int> d_pc_counts_;
 
   // learned candidate ranker
   DevBuf<float2> d_cand_feat_;

@@ -34,8 +34,6 @@ constexpr int kLaneTopK = 32;        // per-lane candidate lists for top_k up to
 constexpr int kSmemEntries = 2048;   // bucket entries held in shared memory
 constexpr int kSmemHeads = 4096;     // bucket hash heads in shared memory
 constexpr int kScoreThreads = 256;
-constexpr int kSelectThreads = 512;
-constexpr int kSelectSmemKeys = 8192;
 constexpr int kSelectMidGroup = 32;   // groups of 9..32 members: a small CTA each
 constexpr int kSelectMidThreads = 128;
 constexpr int kSelectMidKeys = 512;   // >= min(C(32,2), 16 * 32) candidates

@@ -202,6 +202,12 @@ class Engine:
         N.check(N.lib().beam_engine_merge_pairs(self._h, _ptr(keep, C.c_int32), _ptr(remove, C.c_int32),
                                                 len(keep)))
 
+    def exact_partition_cost(self) -> int:
+        """CostOracle::ExactPartitionCost of the current partition, on the device."""
+        out = C.c_int64()
+        N.check(N.lib().beam_engine_exact_partition_cost(self._h, C.byref(out)))
+        return int(out.value)
+
     def ranker_info(self) -> dict:
         info = N.RankerInfo()
         N.check(N.lib().beam_engine_ranker_info(self._h, C.byref(info)))

@@ -181,6 +181,11 @@ int beam_engine_ranker_info(beam_engine* e, beam_ranker_info* out);
 int beam_ranker_grad(int32_t device, const float* x, const float* y, const float* w, int64_t n,
                      const float* params, float* grad, double* loss, float* logits);
 const char* beam_ranker_last_error(void);
+/* CostOracle::ExactPartitionCost (src/cost_oracle.cpp:112-124) of the
+ * engine's current partition, computed on the device from the resident input
+ * graph (sort of supernode-pair keys + run-length encode); the check of
+ * src/main.cpp:560-566 compares it with the encoding payload. */
+int beam_engine_exact_partition_cost(beam_engine* e, int64_t* cost);
 /* QuotientGraph::Nnz (src/quotient_graph.cpp:259-270). */
 int beam_engine_quotient_nnz(beam_engine* e, int64_t* nnz);
 /* CUDA-event timing of every launch of one kernel class (BEAM_TIME_*). */

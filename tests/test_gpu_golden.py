@@ -27,8 +27,11 @@ def gpu_metrics(case, tmp_path):
         labels, head, nxt = e.partition()
         st = e.stats()
         qnnz = e.quotient_nnz()
+        device_cost = e.exact_partition_cost()
     enc = g.encode(head, nxt, tmp_path)
     m = {k: st[k] for k in COUNTERS}
+    # the device ExactPartitionCost must agree with the host one (and the reference's)
+    assert device_cost == g.exact_partition_cost(labels)
     m.update(n=g.n, partition_hash=partition_hash(labels), exact_partition_cost=g.exact_partition_cost(labels),
              supernode_count=enc["supernodes"], P=enc["p"], Cp=enc["cp"], Cm=enc["cm"],
              num_superedges_loop=enc["superedges_loop"], num_superedges_nonloop=enc["superedges_nonloop"],
