@@ -44,8 +44,8 @@ struct RankerInfo {
 // Largest group the kernels accept (bounded by the packed select keys and
 // the per-group pair tables); the reference default is 512.
 constexpr int kMaxGroup = 1024;
-// Persistent grid of the row-update kernel (two CTAs per SM of a GB300).
-constexpr int kRowsGrid = 2 * 152;
+// Persistent grid of the row-update kernels (four CTAs per SM of a GB300).
+constexpr int kRowsGrid = 4 * 152;
 
 void CheckCuda(cudaError_t status, const char* what);
 

@@ -433,11 +433,9 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
       ei[eo + k] = i;
       ee[eo + k] = static_cast<unsigned>(c);
       enx[eo + k] = atomicExch(&heads[BucketHash(t, hmask)], eo + k);
-      if (P.group_of[t] == gid) {
-        const int j = P.idx_in_group[t];
-        if (i < j) atomicAdd(reinterpret_cast<unsigned long long*>(&pmat[static_cast<long long>(i) * g + j]),
-                             static_cast<unsigned long long>(c));
-      }
+      // direct in-group edge: row i holds j and row j holds i with the same
+      // count, so each half of the table gets it once
+      if (P.group_of[t] == gid) pmat[static_cast<long long>(i) * g + P.idx_in_group[t]] = c;
     }
     old = WarpSum(old);
     if (lane == 0) {
@@ -471,20 +469,16 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
       const long long newc = EncodeCostForPair(qa, sa + sb, t, st, ea + eb);
       const long long delta = oldc - newc;
       if (delta > 0) {
+        // both halves, so every member's partners are one contiguous row
         atomicAdd(reinterpret_cast<unsigned long long*>(&pmat[static_cast<long long>(a) * g + b]),
+                  static_cast<unsigned long long>(delta));
+        atomicAdd(reinterpret_cast<unsigned long long*>(&pmat[static_cast<long long>(b) * g + a]),
                   static_cast<unsigned long long>(delta));
       }
     }
   }
   examined = WarpSum(static_cast<long long>(examined));
   if (lane == 0 && examined) atomicAdd(&S.examined, examined);
-  __syncthreads();
-  // mirror the upper triangle so every member's partners are one contiguous row
-  for (long long idx = tid; idx < gg; idx += kPrepThreads) {
-    const int i = static_cast<int>(idx / g);
-    const int j = static_cast<int>(idx - static_cast<long long>(i) * g);
-    if (j < i) pmat[idx] = pmat[static_cast<long long>(j) * g + i];
-  }
   __syncthreads();
   // old costs for the member pass, counters of the group
   long long* old_out = reinterpret_cast<long long*>(mat + OldCostOffset(gg));
@@ -615,6 +609,7 @@ __global__ void __launch_bounds__(kAccumThreads) PrepareAccumKernel(PrepareParam
 // launch's big-group list (moff = prefix of the member counts), so a large
 // group's members are ranked by the whole GPU instead of one CTA.
 __global__ void __launch_bounds__(256) PrepareMembersKernel(PrepareParams P) {
+  __shared__ int cand_j[8][32];  // per warp: the candidates that survive the prescreen
   const int lane = threadIdx.x & 31;
   const long long wg = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const long long total = P.moff[P.list0 + P.nlist] - P.moff[P.list0];
@@ -661,14 +656,99 @@ __global__ void __launch_bounds__(256) PrepareMembersKernel(PrepareParams P) {
       fmat[static_cast<long long>(a) * g + b] = 1;
     }
   } else if (top_k <= kLaneTopK) {
+    // fp32 prescreen: the exact (double) ratio is only computed for the
+    // candidates that can be in the member's top_k. The fp32 ratio of a
+    // candidate is within relative 3 * 2^-24 of its double ratio, so every
+    // candidate of the exact top_k has an fp32 ratio >= tau * (1 - 2^-20),
+    // where tau is the top_k-th largest fp32 ratio (found by bisection on the
+    // float bit patterns, which order like the positive values).
+    float rf[kMaxGroup / 32];
+#pragma unroll
+    for (int t = 0; t < kMaxGroup / 32; ++t) {
+      const int j = lane + 32 * t;
+      float v = 0.0f;  // not a candidate
+      if (j < g && j != i) {
+        const long long pg = prow[j];
+        if (pg > 0) {
+          long long denom = old_i + old[j];
+          if (denom < 1) denom = 1;
+          v = __fdiv_rn(static_cast<float>(pg), static_cast<float>(denom));
+        }
+      }
+      rf[t] = v;
+    }
+    float cut = 0.0f;
+    if (cnt > top_k + 16) {
+      unsigned lo = 0, hi = 0x7f800000u;  // count(bits >= lo) >= top_k > count(bits >= hi)
+      while (hi - lo > 1) {
+        const unsigned mid = lo + ((hi - lo) >> 1);
+        int c = 0;
+#pragma unroll
+        for (int t = 0; t < kMaxGroup / 32; ++t) c += __float_as_uint(rf[t]) >= mid ? 1 : 0;
+        c = WarpSumInt(c);
+        if (c >= top_k) lo = mid; else hi = mid;
+      }
+      cut = __uint_as_float(lo) * (1.0f - 9.5367431640625e-7f);
+    }
+    int npass = 0;
+#pragma unroll
+    for (int t = 0; t < kMaxGroup / 32; ++t) npass += (rf[t] > 0.0f && rf[t] >= cut) ? 1 : 0;
+    npass = WarpSumInt(npass);
+    if (npass <= 32) {
+      // one surviving candidate per lane; its rank is the number of
+      // candidates better than it under the strict order, and the top_k
+      // ranks are kept
+      int* cj = cand_j[threadIdx.x >> 5];
+      int base = 0;
+#pragma unroll
+      for (int t = 0; t < kMaxGroup / 32; ++t) {
+        const bool pass = rf[t] > 0.0f && rf[t] >= cut;
+        const unsigned ball = __ballot_sync(0xffffffffu, pass);
+        if (pass) cj[base + __popc(ball & ((1u << lane) - 1u))] = lane + 32 * t;
+        base += __popc(ball);
+      }
+      __syncwarp();
+      const bool have = lane < npass;
+      RankKey mine;
+      mine.ratio = 0.0;
+      mine.pg = 0;
+      mine.lo = 0;
+      mine.hi = 0;
+      mine.j = -1;
+      if (have) {
+        const int j = cj[lane];
+        const long long pg = prow[j];
+        const int qj = q[j];
+        mine.j = j;
+        mine.ratio = ratio_of(j, pg);
+        mine.pg = pg;
+        mine.lo = qi < qj ? qi : qj;
+        mine.hi = qi < qj ? qj : qi;
+      }
+      int rank = 0;
+      for (int o = 0; o < npass; ++o) {
+        RankKey other;
+        other.ratio = __shfl_sync(0xffffffffu, mine.ratio, o);
+        other.pg = __shfl_sync(0xffffffffu, mine.pg, o);
+        other.lo = __shfl_sync(0xffffffffu, mine.lo, o);
+        other.hi = __shfl_sync(0xffffffffu, mine.hi, o);
+        if (have && o != lane && Better(other, mine)) ++rank;
+      }
+      if (have && rank < top_k) {
+        const int a = i < mine.j ? i : mine.j;
+        const int b = i < mine.j ? mine.j : i;
+        fmat[static_cast<long long>(a) * g + b] = 1;
+      }
+    } else {
     // each lane keeps its best top_k candidates sorted, then the warp merges
     // the 32 lists head by head (candidates are distinct, so no key ties)
     RankKey lst[kLaneTopK];
     int nl = 0;
-    for (int j = lane; j < g; j += 32) {
-      if (j == i) continue;
+#pragma unroll
+    for (int t = 0; t < kMaxGroup / 32; ++t) {
+      const int j = lane + 32 * t;
+      if (rf[t] <= 0.0f || rf[t] < cut) continue;
       const long long pg = prow[j];
-      if (pg <= 0) continue;
       RankKey k;
       k.j = j;
       k.ratio = ratio_of(j, pg);
@@ -713,6 +793,7 @@ __global__ void __launch_bounds__(256) PrepareMembersKernel(PrepareParams P) {
         const int b = i < best.j ? best.j : i;
         fmat[static_cast<long long>(a) * g + b] = 1;
       }
+    }
     }
   } else {
     RankKey prev;
