@@ -287,9 +287,16 @@ void Engine::Divide(int iter) {
   CheckCuda(cudaMemsetAsync(d_head_flag_.p, 0, sizeof(int) * static_cast<size_t>(n), s), "memset");
   ++launches_;
   ScatterActiveKernel<<<Blocks(n, T), T, 0, s>>>(d_qsize_.p, scan, n, d_order_.p, d_head_flag_.p);
-  int last_scan = 0, last_flag = 0;
-  fetch2(scan + n - 1, flags + n - 1, &last_scan, &last_flag);
-  const int count = last_scan + last_flag;
+  // active supernodes: known on the host after a Merge (n - accepted
+  // merges, read back with the Merge's final synchronisation), else read
+  int count = 0;
+  if (known_active_ >= 0) {
+    count = static_cast<int>(known_active_);
+  } else {
+    int last_scan = 0, last_flag = 0;
+    fetch2(scan + n - 1, flags + n - 1, &last_scan, &last_flag);
+    count = last_scan + last_flag;
+  }
   n_active_ = count;
 
   // dim_order: dims stable-sorted by (DimRank, dim)
@@ -304,6 +311,7 @@ void Engine::Divide(int iter) {
 
   int segs = 0;
   if (count > 0) {
+    bool settled = false;  // the loop ended with segs / seg_start / seg_len of the final groups
     for (int depth = 0; depth <= cfg_.divide_hash_dims; ++depth) {
       const bool fallback = depth == cfg_.divide_hash_dims;
       scan_incl(d_head_flag_.p, scan, count);
@@ -314,18 +322,28 @@ void Engine::Divide(int iter) {
                                                      seg_len, unf_flag, unf_len);
       scan_excl(unf_flag, unf_idx, count);
       scan_excl(unf_len, unf_off, count);
-      // one read-back per depth: segments, unfinished segments, their items
-      int* dc = uend + n;
-      ++launches_;
-      DepthCountsKernel<<<1, 1, 0, s>>>(scan + count - 1, unf_idx + count - 1, unf_flag + count - 1,
-                                        unf_off + count - 1, unf_len + count - 1, dc);
-      CheckCuda(cudaMemcpyAsync(h_pin_.p, dc, 3 * sizeof(int), cudaMemcpyDeviceToHost, s), "d2h depth counts");
-      CheckCuda(cudaStreamSynchronize(s), "sync");
+      // segments, unfinished segments and their items: known on the host at
+      // depth 0 (one segment of all active supernodes), one read-back later
       int hc[3];
-      std::memcpy(hc, h_pin_.p, sizeof(hc));
+      if (depth == 0) {
+        hc[0] = 1;
+        hc[1] = count > cfg_.divide_max_group ? 1 : 0;
+        hc[2] = hc[1] ? count : 0;
+      } else {
+        int* dc = uend + n;
+        ++launches_;
+        DepthCountsKernel<<<1, 1, 0, s>>>(scan + count - 1, unf_idx + count - 1, unf_flag + count - 1,
+                                          unf_off + count - 1, unf_len + count - 1, dc);
+        CheckCuda(cudaMemcpyAsync(h_pin_.p, dc, 3 * sizeof(int), cudaMemcpyDeviceToHost, s), "d2h depth counts");
+        CheckCuda(cudaStreamSynchronize(s), "sync");
+        std::memcpy(hc, h_pin_.p, sizeof(hc));
+      }
       segs = hc[0];
       const int nu = hc[1];
-      if (nu == 0) break;
+      if (nu == 0) {
+        settled = true;
+        break;
+      }
       const int items = hc[2];
       ++launches_;
       CompactItemsKernel<<<Blocks(count, T), T, 0, s>>>(scan, seg_start, seg_len, unf_flag, unf_idx, unf_off, count,
@@ -379,16 +397,19 @@ void Engine::Divide(int iter) {
                                                          d_vals_alt_.p, fallback ? 1 : 0, cfg_.divide_max_group,
                                                          d_order_.p, d_head_flag_.p);
     }
-    // final segments are the groups
-    scan_incl(d_head_flag_.p, scan, count);
-    ++launches_;
-    SegStartsKernel<<<Blocks(count, T), T, 0, s>>>(d_head_flag_.p, scan, count, seg_start);
-    int seg_total = 0, dummy = 0;
-    fetch2(scan + count - 1, scan + count - 1, &seg_total, &dummy);
-    segs = seg_total;
-    ++launches_;
-    SegLenKernel<<<Blocks(segs, T), T, 0, s>>>(seg_start, segs, count, cfg_.divide_max_group, seg_len, unf_flag,
-                                               unf_len);
+    // final segments are the groups (already described when the loop
+    // settled; after the fallback depth they are recounted)
+    if (!settled) {
+      scan_incl(d_head_flag_.p, scan, count);
+      ++launches_;
+      SegStartsKernel<<<Blocks(count, T), T, 0, s>>>(d_head_flag_.p, scan, count, seg_start);
+      int seg_total = 0, dummy = 0;
+      fetch2(scan + count - 1, scan + count - 1, &seg_total, &dummy);
+      segs = seg_total;
+      ++launches_;
+      SegLenKernel<<<Blocks(segs, T), T, 0, s>>>(seg_start, segs, count, cfg_.divide_max_group, seg_len, unf_flag,
+                                                 unf_len);
+    }
     d_gent_.ensure(static_cast<size_t>(segs) + 1);
     CheckCuda(cudaMemsetAsync(d_gent_.p, 0, sizeof(unsigned) * static_cast<size_t>(segs), s), "memset gent");
     ++launches_;

@@ -237,6 +237,7 @@ void Engine::Reset() {
   need_stamp_ = 0;
   n_groups_ = -1;
   n_active_ = n_;
+  known_active_ = n_;
   hstats_ = HostStats{};
   RankerReset();
 }

@@ -258,6 +258,7 @@ class Engine {
   PinnedBuf<long long> h_pin_;
   int block_stamp_ = 0;
   int64_t n_active_ = 0;
+  int64_t known_active_ = -1;  // active supernodes known on the host (-1: read it back)
   int64_t n_groups_ = 0;
   HostStats hstats_;
 

@@ -23,6 +23,7 @@
 #include <cub/device/device_radix_sort.cuh>
 
 #include <algorithm>
+#include <cstring>
 
 #include "engine.h"
 
@@ -2618,8 +2619,17 @@ void Engine::Merge(int iter, int total_iterations) {
   ++launches_;
   RelabelKernel<<<(n_ + 255) / 256, 256, 0, stream_>>>(d_label_.p, d_fwd_.p, n_);
   n_groups_ = -1;  // the groups are consumed
+  // accepted merges so far, read back with this synchronisation: the next
+  // Divide knows the active count without a round trip of its own
+  CheckCuda(cudaMemcpyAsync(h_pin_.p + 8, d_stats_.p + kStAccepted, sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, stream_), "d2h accepted");
   CheckCuda(cudaStreamSynchronize(stream_), "merge sync");
   CheckError();
+  {
+    unsigned long long accepted = 0;
+    std::memcpy(&accepted, h_pin_.p + 8, sizeof(accepted));
+    known_active_ = static_cast<int64_t>(n_) - static_cast<int64_t>(accepted);
+  }
   if (cfg_.ranker && !rk_trained_ && iter == cfg_.ranker_train_iters) RankerTrain();
   if (cfg_.ranker && rk_trained_ && iter > cfg_.ranker_train_iters) RankerFinishIteration();
 }
@@ -2721,6 +2731,7 @@ int64_t Engine::PrepareGroup(const int32_t* q, int g, int32_t* a_idx, int32_t* b
 
 void Engine::MergePairs(const int32_t* keep, const int32_t* remove, int64_t count) {
   if (count <= 0) return;
+  known_active_ = -1;
   std::vector<char> seen(static_cast<size_t>(n_), 0);
   for (int64_t i = 0; i < count; ++i) {
     const int k = keep[i], r = remove[i];
