@@ -26,7 +26,7 @@ CLI = PKG / "bin" / "beam"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 REFERENCE_DIR = Path("/root/reference")
 
-CU_SOURCES = ["divide.cu", "merge.cu", "engine.cu", "noalloc.cu", "ranker.cu", "partition_cost.cu"]
+CU_SOURCES = ["divide.cu", "merge.cu", "engine.cu", "noalloc.cu", "ranker.cu", "partition_cost.cu", "encode_gpu.cu"]
 CPP_SOURCES = ["graph.cpp", "encode.cpp"]
 
 

@@ -244,16 +244,13 @@ int Run(int argc, char** argv) {
   // CostOracle::ExactPartitionCost on the device (src/main.cpp:560)
   int64_t exact = 0;
   check(beam_engine_exact_partition_cost(e, &exact));
-  beam_engine_destroy(e);
-
+  // Sweg::Encode on the device, files written by the host
   const auto enc0 = Clock::now();
   beam_encoding enc;
   if (o.write_output) std::filesystem::create_directories(o.out_dir);
-  if (beam_encode(static_cast<int32_t>(n), arcs, beam_graph_row_ptr(g), beam_graph_col_idx(g), head.data(), next.data(),
-                  o.write_output ? o.out_dir.c_str() : nullptr, &enc) != 0) {
-    throw std::runtime_error(beam_encode_last_error());
-  }
+  check(beam_engine_encode(e, o.write_output ? o.out_dir.c_str() : nullptr, &enc));
   const double encode_ms = std::chrono::duration<double, std::milli>(Clock::now() - enc0).count();
+  beam_engine_destroy(e);
   if (enc.encoding_cost_standard != exact) {
     throw std::runtime_error("MAGS-compatible payload cost differs from exact partition cost");
   }

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "beam_gb300.h"
+#include "encode_write.h"
 
 namespace {
 
@@ -32,14 +33,15 @@ struct EdgePair {
   bool operator<(const EdgePair& o) const { return a != o.a ? a < o.a : b < o.b; }
 };
 
-void WritePairs(const std::string& path, const std::vector<EdgePair>& v) {
+void WritePairKeys(const std::string& path, const std::vector<unsigned long long>& v) {
   FILE* f = std::fopen(path.c_str(), "w");
   if (!f) throw std::runtime_error("Failed to open output file: " + path);
   std::string buf;
   buf.reserve(1 << 20);
   char line[32];
-  for (const EdgePair& e : v) {
-    const int k = std::snprintf(line, sizeof(line), "%d\t%d\n", e.a, e.b);
+  for (const unsigned long long key : v) {
+    const int k = std::snprintf(line, sizeof(line), "%d\t%d\n", static_cast<int32_t>(key >> 32),
+                                static_cast<int32_t>(key & 0xffffffffu));
     buf.append(line, static_cast<size_t>(k));
     if (buf.size() > (1u << 20)) {
       std::fwrite(buf.data(), 1, buf.size(), f);
@@ -48,6 +50,10 @@ void WritePairs(const std::string& path, const std::vector<EdgePair>& v) {
   }
   std::fwrite(buf.data(), 1, buf.size(), f);
   std::fclose(f);
+}
+
+unsigned long long PairKey(const EdgePair& e) {
+  return static_cast<unsigned long long>(static_cast<uint32_t>(e.a)) << 32 | static_cast<uint32_t>(e.b);
 }
 
 int64_t BlockCostHost(int64_t sa, int64_t sb, int64_t e, bool internal) {
@@ -60,6 +66,45 @@ int64_t BlockCostHost(int64_t sa, int64_t sb, int64_t e, bool internal) {
 }
 
 }  // namespace
+
+namespace beam {
+
+void FinishEncoding(int32_t n, int64_t arcs, const int32_t* head, const int32_t* next, const EncodeOutput& enc,
+                    const char* out_dir, beam_encoding* out) {
+  if (out_dir) {
+    const std::string dir(out_dir);
+    FILE* f = std::fopen((dir + "/G.txt").c_str(), "w");
+    if (!f) throw std::runtime_error("Failed to open G.txt for writing.");
+    int64_t sid = 0;
+    for (int32_t rep = 0; rep < n; ++rep) {
+      if (head[rep] == -1) continue;
+      std::fprintf(f, "%lld", static_cast<long long>(sid++));
+      for (int32_t v = head[rep]; v != -1; v = next[v]) std::fprintf(f, "\t%d", v);
+      std::fputc('\n', f);
+    }
+    std::fclose(f);
+    WritePairKeys(dir + "/P.txt", enc.P);
+    WritePairKeys(dir + "/Cp.txt", enc.Cp);
+    WritePairKeys(dir + "/Cm.txt", enc.Cm);
+  }
+  if (out) {
+    std::memset(out, 0, sizeof(*out));
+    out->supernodes = enc.supernodes;
+    out->p = static_cast<int64_t>(enc.P.size());
+    out->cp = static_cast<int64_t>(enc.Cp.size());
+    out->cm = static_cast<int64_t>(enc.Cm.size());
+    for (const unsigned long long key : enc.P) out->superedges_loop += (key >> 32) == (key & 0xffffffffu);
+    out->superedges_nonloop = out->p - out->superedges_loop;
+    out->encoding_cost_standard = out->p + out->cp + out->cm;
+    out->encoding_cost_mags_x2 = 2 * out->encoding_cost_standard;
+    const int64_t m = arcs / 2;
+    out->cost_ratio_mags_compatible =
+        m > 0 ? static_cast<double>(out->encoding_cost_mags_x2) / (2.0 * static_cast<double>(m)) : 0.0;
+    out->cost_ratio_standard = m > 0 ? static_cast<double>(out->encoding_cost_standard) / static_cast<double>(m) : 0.0;
+  }
+}
+
+}  // namespace beam
 
 extern "C" {
 
@@ -137,35 +182,15 @@ int beam_encode(int32_t n, int64_t arcs, const int64_t* row_ptr, const int32_t* 
     std::sort(P.begin(), P.end());
     std::sort(Cp.begin(), Cp.end());
     std::sort(Cm.begin(), Cm.end());
-    if (out_dir) {
-      const std::string dir(out_dir);
-      FILE* f = std::fopen((dir + "/G.txt").c_str(), "w");
-      if (!f) throw std::runtime_error("Failed to open G.txt for writing.");
-      for (size_t sid = 0; sid < shead.size(); ++sid) {
-        std::fprintf(f, "%zu", sid);
-        for (int32_t v = shead[sid]; v != -1; v = next[v]) std::fprintf(f, "\t%d", v);
-        std::fputc('\n', f);
-      }
-      std::fclose(f);
-      WritePairs(dir + "/P.txt", P);
-      WritePairs(dir + "/Cp.txt", Cp);
-      WritePairs(dir + "/Cm.txt", Cm);
-    }
-    if (out) {
-      std::memset(out, 0, sizeof(*out));
-      out->supernodes = static_cast<int64_t>(shead.size());
-      out->p = static_cast<int64_t>(P.size());
-      out->cp = static_cast<int64_t>(Cp.size());
-      out->cm = static_cast<int64_t>(Cm.size());
-      for (const EdgePair& e : P) out->superedges_loop += e.a == e.b;
-      out->superedges_nonloop = out->p - out->superedges_loop;
-      out->encoding_cost_standard = out->p + out->cp + out->cm;
-      out->encoding_cost_mags_x2 = 2 * out->encoding_cost_standard;
-      const int64_t m = row_ptr[n] / 2;
-      out->cost_ratio_mags_compatible =
-          m > 0 ? static_cast<double>(out->encoding_cost_mags_x2) / (2.0 * static_cast<double>(m)) : 0.0;
-      out->cost_ratio_standard = m > 0 ? static_cast<double>(out->encoding_cost_standard) / static_cast<double>(m) : 0.0;
-    }
+    beam::EncodeOutput enc;
+    enc.supernodes = static_cast<int64_t>(shead.size());
+    enc.P.reserve(P.size());
+    enc.Cp.reserve(Cp.size());
+    enc.Cm.reserve(Cm.size());
+    for (const EdgePair& e : P) enc.P.push_back(PairKey(e));
+    for (const EdgePair& e : Cp) enc.Cp.push_back(PairKey(e));
+    for (const EdgePair& e : Cm) enc.Cm.push_back(PairKey(e));
+    beam::FinishEncoding(n, row_ptr[n], head, next, enc, out_dir, out);
     return 0;
   } catch (const std::exception& e) {
     g_encode_error = e.what();

@@ -19,6 +19,7 @@
 #include <string>
 
 #include "beam_gb300.h"
+#include "encode_write.h"
 #include "engine.h"
 
 namespace beam {
@@ -671,6 +672,17 @@ int beam_engine_ranker_info(beam_engine* e, beam_ranker_info* out) {
     out->calib_recall = r.calib_recall;
     out->calib_prune = r.calib_prune;
     out->trained = r.trained ? 1 : 0;
+  });
+}
+
+int beam_engine_encode(beam_engine* e, const char* out_dir, beam_encoding* out) {
+  return Guard([&] {
+    const int n = e->impl->n();
+    std::vector<int32_t> labels(static_cast<size_t>(n)), head(static_cast<size_t>(n)), next(static_cast<size_t>(n));
+    e->impl->Partition(labels.data(), head.data(), next.data());
+    beam::EncodeOutput enc;
+    e->impl->Encode(&enc);
+    beam::FinishEncoding(n, e->impl->arcs(), head.data(), next.data(), enc, out_dir, out);
   });
 }
 

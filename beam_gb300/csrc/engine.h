@@ -14,6 +14,8 @@
 
 namespace beam {
 
+struct EncodeOutput;
+
 struct EngineConfig {
   int top_k = 16;
   int group_batch_size = 64;
@@ -141,6 +143,8 @@ class Engine {
   int64_t QuotientNnz();
   // CostOracle::ExactPartitionCost of the current partition, from the input graph.
   int64_t ExactPartitionCost();
+  // Sweg::Encode of the current partition: P (supernode ids), Cp and Cm.
+  void Encode(EncodeOutput* out);
   const HostStats& host_stats() const { return hstats_; }
   const RankerInfo& ranker_info() const { return rk_info_; }
   int64_t active_count() const { return n_active_; }

@@ -202,6 +202,14 @@ class Engine:
         N.check(N.lib().beam_engine_merge_pairs(self._h, _ptr(keep, C.c_int32), _ptr(remove, C.c_int32),
                                                 len(keep)))
 
+    def encode(self, out_dir: str | None = None) -> dict:
+        """Sweg::Encode of the current partition on the device; writes the four
+        files into out_dir when given."""
+        enc = N.Encoding()
+        N.check(N.lib().beam_engine_encode(self._h, None if out_dir is None else str(out_dir).encode(),
+                                           C.byref(enc)))
+        return enc.as_dict()
+
     def exact_partition_cost(self) -> int:
         """CostOracle::ExactPartitionCost of the current partition, on the device."""
         out = C.c_int64()

@@ -241,6 +241,13 @@ typedef struct {
   double cost_ratio_standard, cost_ratio_mags_compatible;
 } beam_encoding;
 
+/* Sweg::Encode (src/sweg.cpp:3017-3163) + WriteOutput (src/sweg.cpp:3255-3287)
+ * of the engine's current partition, computed on the device (pair-key radix
+ * sort, run-length encode, per-block decision, Cm enumeration); writes
+ * G.txt, P.txt, Cp.txt, Cm.txt into out_dir when not NULL. Same files and
+ * metrics as beam_encode. */
+int beam_engine_encode(beam_engine* e, const char* out_dir, beam_encoding* out);
+
 /* Sweg::Encode (mags-compatible) of the partition given as member lists
  * (head[rep] = -1 for inactive reps, next[node]), plus the compression
  * metrics; writes G.txt, P.txt, Cp.txt, Cm.txt into out_dir when not NULL. */

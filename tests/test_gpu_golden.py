@@ -28,10 +28,16 @@ def gpu_metrics(case, tmp_path):
         st = e.stats()
         qnnz = e.quotient_nnz()
         device_cost = e.exact_partition_cost()
+        device_dir = tmp_path / "device"
+        device_dir.mkdir()
+        device_enc = e.encode(device_dir)
     enc = g.encode(head, nxt, tmp_path)
     m = {k: st[k] for k in COUNTERS}
-    # the device ExactPartitionCost must agree with the host one (and the reference's)
+    # the device ExactPartitionCost and Encode must agree with the host ones
+    # (and so with the reference's)
     assert device_cost == g.exact_partition_cost(labels)
+    assert device_enc == enc
+    assert file_hashes(device_dir) == file_hashes(tmp_path)
     m.update(n=g.n, partition_hash=partition_hash(labels), exact_partition_cost=g.exact_partition_cost(labels),
              supernode_count=enc["supernodes"], P=enc["p"], Cp=enc["cp"], Cm=enc["cm"],
              num_superedges_loop=enc["superedges_loop"], num_superedges_nonloop=enc["superedges_nonloop"],
