@@ -74,6 +74,7 @@ enum ErrCode : int {
   kErrKeyRange = 7,         // gain outside the packed sort-key range
   kErrInactive = 8,         // scoring request on an inactive supernode
   kErrSlots = 9,            // a group's row entries exceed its sort slots
+  kErrGraph = 10,           // a neighbour out of range or a self-loop in the input CSR
 };
 
 struct DevError {

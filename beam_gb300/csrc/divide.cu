@@ -242,6 +242,7 @@ inline int Blocks(long long items, int threads) {
 }  // namespace
 
 void Engine::Divide(int iter) {
+  AllocScope alloc(stream_);
   const int n = n_;
   const int T = 256;
   cudaStream_t s = stream_;

@@ -182,6 +182,7 @@ __global__ void EmitDenseKernel(EmitParams E) {
 }  // namespace
 
 void Engine::Encode(EncodeOutput* out) {
+  AllocScope alloc(stream_);
   const int n = n_;
   const long long arcs = arcs_;
   cudaStream_t s = stream_;

@@ -13,16 +13,60 @@
 #include <cub/device/device_reduce.cuh>
 #include <cub/device/device_scan.cuh>
 
+#include <algorithm>
 #include <chrono>
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "beam_gb300.h"
 #include "encode_write.h"
 #include "engine.h"
 
 namespace beam {
+
+namespace {
+thread_local cudaStream_t g_alloc_stream = nullptr;
+std::mutex g_pool_mutex;
+std::vector<int> g_pool_ready;  // devices whose default pool keeps freed memory
+}  // namespace
+
+cudaStream_t CurrentAllocStream() { return g_alloc_stream; }
+
+AllocScope::AllocScope(cudaStream_t s) : prev_(g_alloc_stream) { g_alloc_stream = s; }
+AllocScope::~AllocScope() { g_alloc_stream = prev_; }
+
+void* DeviceAlloc(size_t bytes, cudaStream_t s) {
+  void* p = nullptr;
+  if (s == nullptr) {
+    CheckCuda(cudaMalloc(&p, bytes), "cudaMalloc");
+    return p;
+  }
+  int dev = 0;
+  CheckCuda(cudaGetDevice(&dev), "cudaGetDevice");
+  {
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    if (std::find(g_pool_ready.begin(), g_pool_ready.end(), dev) == g_pool_ready.end()) {
+      cudaMemPool_t pool;
+      CheckCuda(cudaDeviceGetDefaultMemPool(&pool, dev), "default mem pool");
+      uint64_t keep = UINT64_MAX;
+      CheckCuda(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep), "mem pool threshold");
+      g_pool_ready.push_back(dev);
+    }
+  }
+  CheckCuda(cudaMallocAsync(&p, bytes, s), "cudaMallocAsync");
+  return p;
+}
+
+void DeviceFree(void* p, cudaStream_t s) {
+  if (s == nullptr) {
+    cudaFree(p);
+  } else {
+    cudaFreeAsync(p, s);
+  }
+}
 
 void CheckCuda(cudaError_t status, const char* what) {
   if (status != cudaSuccess) {
@@ -50,9 +94,10 @@ __global__ void InitScalarsKernel(int n, int* qsize, long long* qint, int* label
 }
 
 // Warp per node: the sorted CSR row, runs of equal neighbours summed.
+// Also validates the input: every neighbour in [0, n) and no self-loop.
 __global__ void InitRowsKernel(const long long* __restrict__ rowptr, const int* __restrict__ col, int n,
                                Entry* __restrict__ pool, long long* __restrict__ qoff, int* __restrict__ qlen,
-                               int* __restrict__ qcap, int* __restrict__ arc_src) {
+                               int* __restrict__ qcap, int* __restrict__ arc_src, DevError* err) {
   const int lane = threadIdx.x & 31;
   const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const long long nw = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
@@ -68,6 +113,7 @@ __global__ void InitRowsKernel(const long long* __restrict__ rowptr, const int* 
         id = col[k];
         arc_src[k] = static_cast<int>(u);
         first = k == s || col[k - 1] != id;
+        if (id < 0 || id >= n || id == u) RaiseError(err, kErrGraph, static_cast<int>(u), id, 0);
       }
       const unsigned ball = __ballot_sync(0xffffffffu, first);
       if (first) {
@@ -128,16 +174,11 @@ Engine::Engine(int n, int64_t arcs, const int64_t* row_ptr, const int32_t* col_i
     throw std::invalid_argument("--divide-max-group above " + std::to_string(kMaxGroup) + " is not supported");
   }
   if (cfg_.group_batch_size < 1) cfg_.group_batch_size = 1;
-  for (int u = 0; u < n; ++u) {
-    for (int64_t k = row_ptr[u]; k < row_ptr[u + 1]; ++k) {
-      const int v = col_idx[k];
-      if (v < 0 || v >= n || v == u) {
-        throw std::invalid_argument("QuotientGraph requires a loop-free graph with valid neighbors");
-      }
-    }
-  }
+  // neighbour range and self-loops are checked on the device (InitRowsKernel)
   CheckCuda(cudaSetDevice(cfg_.device), "cudaSetDevice");
-  CheckCuda(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+  CheckCuda(cudaStreamCreateWithFlags(&owned_stream_.s, cudaStreamNonBlocking), "cudaStreamCreate");
+  stream_ = owned_stream_.s;
+  AllocScope alloc(stream_);
   const size_t un = static_cast<size_t>(n);
   d_rowptr_.ensure(un + 1);
   d_col_.ensure(static_cast<size_t>(arcs) + 1);
@@ -216,24 +257,26 @@ Engine::~Engine() {
   d_stats_.release();
   d_err_.release();
   h_pin_.release();
-  if (stream_) cudaStreamDestroy(stream_);
+  // the stream itself goes with owned_stream_, after every member buffer
 }
 
 void Engine::Reset() {
+  AllocScope alloc(stream_);
   const int T = 256;
   cur_pool_ = 0;
   ++launches_;
   InitScalarsKernel<<<(n_ + T - 1) / T, T, 0, stream_>>>(n_, d_qsize_.p, d_qint_.p, d_label_.p, d_head_.p,
                                                           d_next_.p, d_tail_.p, d_fwd_.p, d_stamp_.p, d_partner_.p,
                                                           d_claim_.p, d_need_.p);
+  CheckCuda(cudaMemsetAsync(d_err_.p, 0, sizeof(DevError), stream_), "memset err");
   ++launches_;
   InitRowsKernel<<<152 * 16, 256, 0, stream_>>>(d_rowptr_.p, d_col_.p, n_, d_pool_[0].p, d_qoff_.p, d_qlen_.p,
-                                                d_qcap_.p, d_arc_src_.p);
+                                                d_qcap_.p, d_arc_src_.p, d_err_.p);
   const unsigned long long top = static_cast<unsigned long long>(arcs_);
   CheckCuda(cudaMemcpyAsync(d_pool_top_.p, &top, sizeof(top), cudaMemcpyHostToDevice, stream_), "h2d pool top");
   CheckCuda(cudaMemsetAsync(d_stats_.p, 0, sizeof(unsigned long long) * kStCount, stream_), "memset stats");
-  CheckCuda(cudaMemsetAsync(d_err_.p, 0, sizeof(DevError), stream_), "memset err");
   CheckCuda(cudaStreamSynchronize(stream_), "reset sync");
+  CheckError();
   block_stamp_ = 0;
   need_stamp_ = 0;
   n_groups_ = -1;
@@ -258,6 +301,10 @@ void Engine::CheckError() {
     case kErrKeyRange: msg = "merge gain outside the selection key range"; break;
     case kErrInactive: msg = "quotient supernode is inactive or endpoints are equal"; break;
     case kErrSlots: msg = "group row entries exceed their prepare sort slots"; break;
+    case kErrGraph:
+      msg = "QuotientGraph requires a loop-free graph with valid neighbors";
+      CheckCuda(cudaMemset(d_err_.p, 0, sizeof(DevError)), "memset err");
+      throw std::invalid_argument(msg);
     default: msg = "device error"; break;
   }
   msg += " (" + std::to_string(e.a) + ", " + std::to_string(e.b) + ", " + std::to_string(e.c) + ")";
@@ -299,6 +346,7 @@ void Engine::CompactPool() {
 }
 
 void Engine::Run(int iterations) {
+  AllocScope alloc(stream_);
   using Clock = std::chrono::steady_clock;
   const auto t0 = Clock::now();
   for (int iter = 1; iter <= iterations; ++iter) {
@@ -372,6 +420,7 @@ void Engine::DeviceStats(uint64_t* out, int count) {
 }
 
 int64_t Engine::QuotientNnz() {
+  AllocScope alloc(stream_);
   DevBuf<long long> lens, sum;
   const int T = 256;
   lens.ensure(static_cast<size_t>(n_));
@@ -439,6 +488,7 @@ double Engine::StepTimerStopMs() {
 }
 
 void Engine::FlushL2() {
+  AllocScope alloc(stream_);
   const size_t bytes = static_cast<size_t>(256) << 20;  // twice the 129 MB L2 of a GB300
   d_flush_.ensure(bytes);
   CheckCuda(cudaMemsetAsync(d_flush_.p, static_cast<int>(launches_ & 0xff), bytes, stream_), "l2 flush");

@@ -51,10 +51,30 @@ constexpr int kRowsGrid = 4 * 152;
 
 void CheckCuda(cudaError_t status, const char* what);
 
+// Device memory. Inside an AllocScope (every engine call sets one for its
+// stream) buffers come from the device's stream-ordered pool, which keeps
+// freed memory for the next allocation, so creating, growing and destroying
+// engines pays no cudaMalloc / cudaFree; outside one, plain cudaMalloc.
+cudaStream_t CurrentAllocStream();
+void* DeviceAlloc(size_t bytes, cudaStream_t s);
+void DeviceFree(void* p, cudaStream_t s);
+
+class AllocScope {
+ public:
+  explicit AllocScope(cudaStream_t s);
+  ~AllocScope();
+  AllocScope(const AllocScope&) = delete;
+  AllocScope& operator=(const AllocScope&) = delete;
+
+ private:
+  cudaStream_t prev_;
+};
+
 template <typename T>
 struct DevBuf {
   T* p = nullptr;
   size_t n = 0;
+  cudaStream_t s = nullptr;  // stream of a pool allocation (nullptr: cudaMalloc)
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
@@ -63,13 +83,30 @@ struct DevBuf {
     if (count <= n) return;
     release();
     const size_t bytes = (count ? count : 1) * sizeof(T);
-    CheckCuda(cudaMalloc(reinterpret_cast<void**>(&p), bytes), "cudaMalloc");
+    s = CurrentAllocStream();
+    p = static_cast<T*>(DeviceAlloc(bytes, s));
     n = count;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) DeviceFree(p, s);
     p = nullptr;
     n = 0;
+    s = nullptr;
+  }
+};
+
+// The engine's stream, destroyed after every buffer of the engine is freed
+// (declared before them).
+struct OwnedStream {
+  cudaStream_t s = nullptr;
+  OwnedStream() = default;
+  OwnedStream(const OwnedStream&) = delete;
+  OwnedStream& operator=(const OwnedStream&) = delete;
+  ~OwnedStream() {
+    if (s) {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+    }
   }
 };
 
@@ -192,6 +229,7 @@ class Engine {
   int n_;
   int64_t arcs_;
   EngineConfig cfg_;
+  OwnedStream owned_stream_;
   cudaStream_t stream_ = nullptr;
 
   // graph

@@ -2608,6 +2608,7 @@ void Engine::RunBlock(size_t b, double threshold, int iter, int total_iterations
 }
 
 void Engine::Merge(int iter, int total_iterations) {
+  AllocScope alloc(stream_);
   if (n_groups_ < 0) throw std::runtime_error("Merge requires a preceding Divide");
   // ComputeMergeThreshold, reciprocal policy (src/sweg.cpp:400-406)
   const double threshold = 1.0 / static_cast<double>(iter + 1);
@@ -2636,6 +2637,7 @@ void Engine::Merge(int iter, int total_iterations) {
 
 void Engine::ScorePairs(const int32_t* rep_a, const int32_t* rep_b, int64_t count, int64_t* gain,
                         int64_t* before) {
+  AllocScope alloc(stream_);
   if (count <= 0) return;
   for (int64_t i = 0; i < count; ++i) {
     if (rep_a[i] < 0 || rep_a[i] >= n_ || rep_b[i] < 0 || rep_b[i] >= n_) {
@@ -2669,6 +2671,7 @@ void Engine::ScorePairs(const int32_t* rep_a, const int32_t* rep_b, int64_t coun
 }
 
 int64_t Engine::PrepareGroup(const int32_t* q, int g, int32_t* a_idx, int32_t* b_idx, int64_t cap) {
+  AllocScope alloc(stream_);
   if (g < 0 || g > kMaxGroup) throw std::invalid_argument("group size out of range");
   std::vector<int> hq(q, q + g);
   for (int i = 0; i < g; ++i) {
@@ -2730,6 +2733,7 @@ int64_t Engine::PrepareGroup(const int32_t* q, int g, int32_t* a_idx, int32_t* b
 }
 
 void Engine::MergePairs(const int32_t* keep, const int32_t* remove, int64_t count) {
+  AllocScope alloc(stream_);
   if (count <= 0) return;
   known_active_ = -1;
   std::vector<char> seen(static_cast<size_t>(n_), 0);

@@ -56,6 +56,7 @@ __global__ void PairCostKernel(const unsigned long long* __restrict__ uniq, cons
 }  // namespace
 
 int64_t Engine::ExactPartitionCost() {
+  AllocScope alloc(stream_);
   const long long arcs = arcs_;
   cudaStream_t s = stream_;
   d_pc_keys_[0].ensure(static_cast<size_t>(arcs) + 1);

@@ -57,3 +57,21 @@ def test_merge_requires_divide():
     with Engine(g) as e:
         with pytest.raises(BeamError, match="Divide"):
             e.merge(1)
+
+
+class RawCSR:
+    def __init__(self, row_ptr, col_idx):
+        import numpy as np
+        self.row_ptr = np.asarray(row_ptr, np.int64)
+        self.col_idx = np.asarray(col_idx, np.int32)
+        self.n = len(row_ptr) - 1
+        self.arcs = len(col_idx)
+
+
+@pytest.mark.parametrize("row_ptr,col_idx", [([0, 2, 3, 4], [0, 1, 0, 0]),    # self-loop 0-0
+                                             ([0, 1, 2, 3], [1, 7, 0])])      # neighbour out of range
+def test_engine_rejects_invalid_csr_on_the_device(row_ptr, col_idx):
+    from beam_gb300 import Engine
+    from beam_gb300._native import BeamError
+    with pytest.raises(BeamError, match="loop-free graph with valid neighbors"):
+        Engine(RawCSR(row_ptr, col_idx))
