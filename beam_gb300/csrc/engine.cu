@@ -208,6 +208,7 @@ Engine::Engine(int n, int64_t arcs, const int64_t* row_ptr, const int32_t* col_i
   d_keys_.ensure(un + 1);
   d_keys_alt_.ensure(un + 1);
   d_ctl_.ensure(1);
+  d_rw_ticket_.ensure(1);
   d_stats_.ensure(kStCount);
   d_err_.ensure(1);
   d_scratch_.ensure((static_cast<size_t>(64) << 20) + 32 * (static_cast<size_t>(arcs) + un));
@@ -269,6 +270,8 @@ void Engine::Reset() {
                                                           d_next_.p, d_tail_.p, d_fwd_.p, d_stamp_.p, d_partner_.p,
                                                           d_claim_.p, d_need_.p);
   CheckCuda(cudaMemsetAsync(d_err_.p, 0, sizeof(DevError), stream_), "memset err");
+  CheckCuda(cudaMemsetAsync(d_ctl_.p, 0, sizeof(BlockCtl), stream_), "memset ctl");
+  CheckCuda(cudaMemsetAsync(d_rw_ticket_.p, 0, sizeof(unsigned), stream_), "memset ticket");
   ++launches_;
   InitRowsKernel<<<152 * 16, 256, 0, stream_>>>(d_rowptr_.p, d_col_.p, n_, d_pool_[0].p, d_qoff_.p, d_qlen_.p,
                                                 d_qcap_.p, d_arc_src_.p, d_err_.p);

@@ -133,8 +133,6 @@ struct PinnedBuf {
 
 // Per-block control words, reset before every 64-group block.
 struct BlockCtl {
-  unsigned int acc_cnt;     // accepted merges in the block
-  unsigned int aff_cnt;     // neighbour rows to rewrite
   unsigned long long scratch_top;  // bump pointer into the block scratch (bytes)
   unsigned int short_cnt;   // claimed neighbour rows rewritten by one warp each
   unsigned int long_cnt;    // claimed neighbour rows rewritten by one CTA each
@@ -252,6 +250,7 @@ class Engine {
   DevBuf<int> d_label_, d_head_, d_next_, d_tail_, d_fwd_;
   DevBuf<int> d_stamp_, d_partner_, d_claim_, d_seq_;
   DevBuf<int> d_rows_short_, d_rows_long_;  // claimed neighbour rows of a block
+  DevBuf<unsigned> d_rw_ticket_;             // last-CTA counter of the rewrite kernel
 
   // divide
   DevBuf<int> d_order_, d_head_flag_;

@@ -35,6 +35,7 @@ constexpr int kLaneTopK = 32;        // per-lane candidate lists for top_k up to
 constexpr int kSmemEntries = 2048;   // bucket entries held in shared memory
 constexpr int kSmemHeads = 4096;     // bucket hash heads in shared memory
 constexpr int kScoreThreads = 256;
+constexpr int kFewGroups = 256;  // blocks of at most this many groups take fewer, wider launches
 constexpr int kSelectMidGroup = 32;   // groups of 9..32 members: a small CTA each
 constexpr int kSelectMidThreads = 128;
 constexpr int kSelectMidKeys = 512;   // >= min(C(32,2), 16 * 32) candidates
@@ -1533,7 +1534,8 @@ __global__ void __launch_bounds__(kMatchThreads) SelectMatchKernel(SelectParams 
   __shared__ unsigned long long* gkeys;
   __shared__ unsigned long long rej_thr;
   const int tid = threadIdx.x;
-  const int ri = P.list[P.list0 + blockIdx.x];
+  // list == nullptr: the real groups list0, list0 + 1, ... (a whole block)
+  const int ri = P.list ? P.list[P.list0 + blockIdx.x] : P.list0 + static_cast<int>(blockIdx.x);
   const int gid = P.real[ri];
   const int g = P.glen[gid];
   const int cnt = g >= 2 && g <= kMaxGroup ? P.cand_cnt[ri] : 0;
@@ -1826,6 +1828,7 @@ struct CommitParams {
   DevError* err;
   int* rows_short;  // claimed neighbour rows of at most kWarpRow entries (count: ctl->short_cnt)
   int* rows_long;   // the other claimed neighbour rows (count: ctl->long_cnt)
+  unsigned* ticket; // last-CTA counter of the rewrite kernel, left at 0
 };
 
 // Optional re-validation (--verify-cuda-gain): recomputes the exact gain of
@@ -2164,8 +2167,21 @@ __device__ void RewriteLongRows(const CommitParams& P, RowsSmem& R) {
 __global__ void __launch_bounds__(kRowsThreads) RewriteRowsKernel(CommitParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   RowsSmem& R = *reinterpret_cast<RowsSmem*>(smem_raw);
+  __shared__ bool last;
   RewriteLongRows(P, R);
   RewriteShortRows(P);
+  // the last CTA to finish clears the block control words for the next
+  // block (every CTA has read them and made its scratch allocations by now)
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(P.ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    P.ctl->scratch_top = 0;
+    P.ctl->short_cnt = 0;
+    P.ctl->long_cnt = 0;
+    *P.ticket = 0u;
+  }
 }
 
 __global__ void ScatterGroupKernel(const int* __restrict__ q, const int* __restrict__ idx, int g,
@@ -2236,16 +2252,26 @@ void Engine::PrepareIterationBuffers() {
   h_soff_.assign(1, 0);
   h_block_small_.clear();
   h_block_big_.clear();
+  auto is_small = [&](int ri) {
+    const size_t gid = static_cast<size_t>(h_real_[static_cast<size_t>(ri)]);
+    return h_glen_[gid] <= kSmallGroup && h_gent_[gid] <= static_cast<unsigned>(kSmallStage);
+  };
   for (size_t b = 0; b + 1 < h_block_rg_.size(); ++b) {
     h_block_small_.push_back(static_cast<int>(h_small_.size()));
     h_block_big_.push_back(static_cast<int>(h_big_.size()));
+    // a small block with any big group sends all its groups to the big path
+    // (one prepare path, fewer launches; the same candidates)
+    bool all_big = false;
+    if (h_block_rg_[b + 1] - h_block_rg_[b] <= kFewGroups) {
+      for (int ri = h_block_rg_[b]; ri < h_block_rg_[b + 1] && !all_big; ++ri) all_big = !is_small(ri);
+    }
     long long off = 0;
     for (int ri = h_block_rg_[b]; ri < h_block_rg_[b + 1]; ++ri) {
       const size_t gid = static_cast<size_t>(h_real_[static_cast<size_t>(ri)]);
       const long long g = h_glen_[gid];
       // rows counted at Divide time (rows of supernodes not merged yet only
       // shrink during an iteration, so the count is an upper bound)
-      if (g <= kSmallGroup && h_gent_[gid] <= static_cast<unsigned>(kSmallStage)) {
+      if (!all_big && is_small(ri)) {
         h_small_.push_back(ri);
         continue;
       }
@@ -2403,6 +2429,7 @@ void Engine::LaunchCommit(int rg0, int nrg, int64_t max_pairs, bool verify) {
   C.err = d_err_.p;
   C.rows_short = d_rows_short_.p;
   C.rows_long = d_rows_long_.p;
+  C.ticket = d_rw_ticket_.p;
   if (verify) {
     const int vb = static_cast<int>(std::min<int64_t>((max_pairs + 7) / 8 + 1, 152 * 8));
     ++launches_;
@@ -2504,7 +2531,8 @@ void Engine::RunBlock(size_t b, double threshold, int iter, int total_iterations
   const int nrg = rg1 - rg0;
   const long long slots = h_cand_off_[static_cast<size_t>(rg1)] - h_cand_off_[static_cast<size_t>(rg0)];
   const long long sel_slots = h_sel_off_[static_cast<size_t>(rg1)] - h_sel_off_[static_cast<size_t>(rg0)];
-  CheckCuda(cudaMemsetAsync(d_ctl_.p, 0, sizeof(BlockCtl), stream_), "memset ctl");
+  // the block control words are zero: cleared by Merge before the first
+  // block and by the previous block's rewrite kernel
   LaunchPrepare(h_block_small_[b], h_block_small_[b + 1], h_block_big_[b], h_block_big_[b + 1]);
   ScoreParams SP;
   SP.Q = View();
@@ -2581,6 +2609,16 @@ void Engine::RunBlock(size_t b, double threshold, int iter, int total_iterations
   LP.err = d_err_.p;
   const int ss0 = h_block_sel_small_[b], ss1 = h_block_sel_small_[b + 1];
   const int sb0 = h_block_sel_big_[b], sb1 = h_block_sel_big_[b + 1];
+  if (nrg <= kFewGroups) {
+    // a small block: one launch, a CTA per group (same selection)
+    LP.list = nullptr;
+    LP.list0 = rg0;
+    LP.nlist = nrg;
+    ++launches_;
+    SelectMatchKernel<<<nrg, kMatchThreads, 8 * kMatchSmemKeys, stream_>>>(LP);
+    LaunchCommit(rg0, nrg, sel_slots, cfg_.verify_cuda_gain);
+    return;
+  }
   if (ss1 > ss0) {
     LP.list = d_sel_small_.p;
     LP.list0 = ss0;
@@ -2614,6 +2652,7 @@ void Engine::Merge(int iter, int total_iterations) {
   const double threshold = 1.0 / static_cast<double>(iter + 1);
   EnsurePoolRoom();
   PrepareIterationBuffers();
+  CheckCuda(cudaMemsetAsync(d_ctl_.p, 0, sizeof(BlockCtl), stream_), "memset ctl");
   for (size_t b = 0; b + 1 < h_block_rg_.size(); ++b) {
     if (h_block_rg_[b + 1] > h_block_rg_[b]) RunBlock(b, threshold, iter, total_iterations);
   }
