@@ -1524,7 +1524,7 @@ __global__ void __launch_bounds__(kThreads) SelectKernel(SelectParams P) {
 constexpr int kMatchThreads = 512;
 constexpr int kMatchSmemKeys = 8192;
 
-__global__ void __launch_bounds__(kMatchThreads) SelectMatchKernel(SelectParams P) {
+__device__ __forceinline__ void SelectMatchGroup(const SelectParams& P, int ri) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   unsigned long long* skeys = reinterpret_cast<unsigned long long*>(smem_raw);
   __shared__ unsigned long long best[kMaxGroup];
@@ -1534,8 +1534,6 @@ __global__ void __launch_bounds__(kMatchThreads) SelectMatchKernel(SelectParams 
   __shared__ unsigned long long* gkeys;
   __shared__ unsigned long long rej_thr;
   const int tid = threadIdx.x;
-  // list == nullptr: the real groups list0, list0 + 1, ... (a whole block)
-  const int ri = P.list ? P.list[P.list0 + blockIdx.x] : P.list0 + static_cast<int>(blockIdx.x);
   const int gid = P.real[ri];
   const int g = P.glen[gid];
   const int cnt = g >= 2 && g <= kMaxGroup ? P.cand_cnt[ri] : 0;
@@ -1675,6 +1673,11 @@ __global__ void __launch_bounds__(kMatchThreads) SelectMatchKernel(SelectParams 
     atomicAdd(&P.stats[kStValidationWork], best[1]);
     atomicAdd(&P.stats[kStIsolatedGain], total);
   }
+}
+
+__global__ void __launch_bounds__(kMatchThreads) SelectMatchKernel(SelectParams P) {
+  // list == nullptr: the real groups list0, list0 + 1, ... (a whole block)
+  SelectMatchGroup(P, P.list ? P.list[P.list0 + blockIdx.x] : P.list0 + static_cast<int>(blockIdx.x));
 }
 
 // Groups of at most kSelectSmallGroup members (at most 28 candidates): one
