@@ -201,7 +201,8 @@ Engine::Engine(int n, int64_t arcs, const int64_t* row_ptr, const int32_t* col_i
   for (DevBuf<int>* b : {&d_label_, &d_head_, &d_next_, &d_tail_, &d_fwd_, &d_stamp_, &d_partner_, &d_claim_, &d_seq_,
                          &d_order_, &d_head_flag_, &d_vals_, &d_vals_alt_, &d_need_, &d_seg_beg_,
                          &d_seg_end_, &d_pos_map_, &d_gstart_, &d_glen_, &d_group_of_, &d_idx_in_group_,
-                         &d_perm_, &d_perm_alt_, &d_segkey_, &d_segkey_alt_, &d_rows_short_, &d_rows_long_}) {
+                         &d_perm_, &d_perm_alt_, &d_segkey_, &d_segkey_alt_, &d_rows_short_, &d_rows_long_,
+                         &d_sel_list_}) {
     b->ensure(un + 1);
   }
   d_hash_.ensure(un + 1);

@@ -136,6 +136,8 @@ struct BlockCtl {
   unsigned long long scratch_top;  // bump pointer into the block scratch (bytes)
   unsigned int short_cnt;   // claimed neighbour rows rewritten by one warp each
   unsigned int long_cnt;    // claimed neighbour rows rewritten by one CTA each
+  unsigned int sel_total;   // selected pairs of the block (entries of the selection list)
+  unsigned int pad;
 };
 
 struct HostStats {
@@ -250,6 +252,7 @@ class Engine {
   DevBuf<int> d_label_, d_head_, d_next_, d_tail_, d_fwd_;
   DevBuf<int> d_stamp_, d_partner_, d_claim_, d_seq_;
   DevBuf<int> d_rows_short_, d_rows_long_;  // claimed neighbour rows of a block
+  DevBuf<int> d_sel_list_;                   // selection slots of a block's selected pairs
   DevBuf<unsigned> d_rw_ticket_;             // last-CTA counter of the rewrite kernel
 
   // divide

@@ -1364,6 +1364,7 @@ struct SelectParams {
   const int* list;  // real-group positions handled by this launch
   int list0;
   int nlist;
+  int* sel_list;    // selection slots of the selected pairs, appended (count: ctl->sel_total)
 };
 
 // In-place ascending bitonic sort of n (power of two) keys by one CTA.
@@ -1493,6 +1494,7 @@ __global__ void __launch_bounds__(kThreads) SelectKernel(SelectParams P) {
       P.partner[keep] = rem;
       P.partner[rem] = keep;
       P.seq[rem] = static_cast<int>(so + ns);
+      P.sel_list[atomicAdd(&P.ctl->sel_total, 1u)] = static_cast<int>(so + ns);
       work += static_cast<unsigned long long>(P.qlen[keep] + P.qlen[rem]);
       ++ns;
       total += gain;
@@ -1643,6 +1645,7 @@ __device__ __forceinline__ void SelectMatchGroup(const SelectParams& P, int ri) 
     P.partner[keep] = rem;
     P.partner[rem] = keep;
     P.seq[rem] = static_cast<int>(so + i);
+    P.sel_list[atomicAdd(&P.ctl->sel_total, 1u)] = static_cast<int>(so + i);
     my_work += static_cast<unsigned long long>(P.qlen[keep] + P.qlen[rem]);
     my_total += gain;
   }
@@ -1766,6 +1769,7 @@ __global__ void __launch_bounds__(kSelectSmallWarps * 32) SelectSmallKernel(Sele
         P.partner[keep] = rem;
         P.partner[rem] = keep;
         P.seq[rem] = static_cast<int>(so + ns);
+        P.sel_list[atomicAdd(&P.ctl->sel_total, 1u)] = static_cast<int>(so + ns);
         work += static_cast<unsigned long long>(P.qlen[keep] + P.qlen[rem]);
       }
       ++ns;
@@ -1832,20 +1836,20 @@ struct CommitParams {
   int* rows_short;  // claimed neighbour rows of at most kWarpRow entries (count: ctl->short_cnt)
   int* rows_long;   // the other claimed neighbour rows (count: ctl->long_cnt)
   unsigned* ticket; // last-CTA counter of the rewrite kernel, left at 0
+  const int* sel_list;  // selection slots of the block's selected pairs (count: ctl->sel_total)
+  int warp_pairs;       // 1: pairs with at most kWarpRow row entries go to CommitShortKernel
 };
 
 // Optional re-validation (--verify-cuda-gain): recomputes the exact gain of
 // every selected pair against the block-start state and checks it equals
 // the scored gain and is positive.
 __global__ void __launch_bounds__(256) VerifyKernel(CommitParams P) {
-  const long long s0 = P.sel_off[P.rg0];
-  const long long s1 = P.sel_off[P.rg0 + P.nrg];
   const int lane = threadIdx.x & 31;
   const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const long long nw = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
-  for (long long slot = s0 + warp; slot < s1; slot += nw) {
-    const int ri = OwnerOfSlot(P.sel_off, P.rg0, P.rg0 + P.nrg, slot);
-    if (slot - P.sel_off[ri] >= P.sel_cnt[ri]) continue;
+  const unsigned total = P.ctl->sel_total;
+  for (long long idx = warp; idx < total; idx += nw) {
+    const long long slot = P.sel_list[idx];
     const int k = P.sel_keep[slot];
     const int r = P.sel_rem[slot];
     long long gain = 0, before = 0;
@@ -1856,7 +1860,7 @@ __global__ void __launch_bounds__(256) VerifyKernel(CommitParams P) {
 
 // Marks the endpoints of an explicit merge batch (no selection step).
 __global__ void MarkKernel(const int* keep, const int* rem, int count, int* stamp, int* partner, int* seq,
-                           int block_stamp) {
+                           int block_stamp, int* sel_list, BlockCtl* ctl) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < count) {
     stamp[keep[i]] = 2 * block_stamp;
@@ -1864,7 +1868,9 @@ __global__ void MarkKernel(const int* keep, const int* rem, int count, int* stam
     partner[keep[i]] = rem[i];
     partner[rem[i]] = keep[i];
     seq[rem[i]] = i;
+    sel_list[i] = i;
   }
+  if (i == 0) ctl->sel_total = static_cast<unsigned>(count);
 }
 
 struct RowsSmem {
@@ -1993,19 +1999,18 @@ __global__ void __launch_bounds__(kRowsThreads) CommitKernel(CommitParams P) {
   __shared__ long long new_off;
   __shared__ int folded_sum;
   const QuotientView& Q = P.Q;
-  const long long s0 = P.sel_off[P.rg0];
-  const long long s1 = P.sel_off[P.rg0 + P.nrg];
   const int tid = threadIdx.x;
   const int remove_stamp = 2 * P.block_stamp + 1;
-  for (long long slot = s0 + blockIdx.x; slot < s1; slot += gridDim.x) {
-    const int ri = OwnerOfSlot(P.sel_off, P.rg0, P.rg0 + P.nrg, slot);
-    if (slot - P.sel_off[ri] >= P.sel_cnt[ri]) continue;
+  const unsigned total = P.ctl->sel_total;
+  for (unsigned idx = blockIdx.x; idx < total; idx += gridDim.x) {
+    const long long slot = P.sel_list[idx];
     const int k = P.sel_keep[slot];
     const int r = P.sel_rem[slot];
-    const Entry* rr = Q.ent + Q.off[r];
-    const Entry* rk = Q.ent + Q.off[k];
     const int lr = Q.len[r];
     const int lk = Q.len[k];
+    if (P.warp_pairs && lk + lr <= kWarpRow) continue;  // CommitShortKernel's pair
+    const Entry* rr = Q.ent + Q.off[r];
+    const Entry* rk = Q.ent + Q.off[k];
     const int my_seq = static_cast<int>(slot);
     if (tid == 0) folded_sum = 0;
     __syncthreads();
@@ -2081,6 +2086,115 @@ __global__ void __launch_bounds__(kRowsThreads) CommitKernel(CommitParams P) {
       atomicAdd(&P.stats[kStUpdateBytes], 8ull * (2ull * L + nl));
     }
     __syncthreads();
+  }
+}
+
+// Selected pairs whose keep and remove rows hold at most kWarpRow entries
+// together, one warp per pair: the same work as CommitKernel (claims,
+// touched-entry replay, keep row = the two rows with this block's removes
+// renamed to their keeps, ids k and r dropped, equal neighbours summed,
+// Update_S bookkeeping), with the keep row built in registers (bitonic sort
+// across the lanes, segmented sum, compaction).
+__global__ void __launch_bounds__(256) CommitShortKernel(CommitParams P) {
+  const QuotientView& Q = P.Q;
+  const int lane = threadIdx.x & 31;
+  const int remove_stamp = 2 * P.block_stamp + 1;
+  const unsigned total = P.ctl->sel_total;
+  const long long nw = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
+  for (long long idx = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; idx < total;
+       idx += nw) {
+    const long long slot = P.sel_list[idx];
+    const int k = P.sel_keep[slot];
+    const int r = P.sel_rem[slot];
+    const int lr = Q.len[r];
+    const int lk = Q.len[k];
+    if (lk + lr > kWarpRow) continue;  // CommitKernel's pair
+    const Entry* rr = Q.ent + Q.off[r];
+    const Entry* rk = Q.ent + Q.off[k];
+    const int my_seq = static_cast<int>(slot);
+    // touched count and neighbour-row claims (lanes over the remove row)
+    int folded = 0;
+    if (lane < lr) {
+      const int x = EntNb(rr[lane]);
+      if (x != k) {
+        const int sx = P.stamp[x];
+        if (sx == remove_stamp && P.seq[x] < my_seq && RowLookup(rr, lr, P.partner[x]) != 0) folded = 1;
+        if ((sx >> 1) != P.block_stamp && atomicExch(&P.claim[x], P.block_stamp) != P.block_stamp) {
+          if (Q.len[x] <= kWarpRow) {
+            P.rows_short[atomicAdd(&P.ctl->short_cnt, 1u)] = x;
+          } else {
+            P.rows_long[atomicAdd(&P.ctl->long_cnt, 1u)] = x;
+          }
+        }
+      }
+    }
+    const int folded_sum = __popc(__ballot_sync(0xffffffffu, folded != 0));
+    // the keep row: lane i < lk holds row k's entry i, lane lk + j row r's entry j
+    unsigned long long key = ~0ull;
+    long long ekr = 0;
+    if (lane < lk + lr) {
+      const Entry e = lane < lk ? rk[lane] : rr[lane - lk];
+      int id = EntNb(e);
+      if (lane < lk && id == r) ekr = EntCnt(e);
+      if (id != k && id != r) {
+        if (P.stamp[id] == remove_stamp) id = P.partner[id];
+        key = static_cast<unsigned long long>(id) << 32 | static_cast<unsigned long long>(EntCnt(e));
+      }
+    }
+    ekr = WarpMax(ekr);
+    key = WarpBitonicSortAsc(key, lane);
+    const bool valid = key != ~0ull;
+    const int id = static_cast<int>(key >> 32);
+    const long long c = valid ? static_cast<long long>(key & 0xffffffffull) : 0;
+    const int prev = __shfl_up_sync(0xffffffffu, id, 1);
+    const bool head = valid && (lane == 0 || prev != id);
+    long long sum = c;
+    bool more = head;
+    for (int j = 1; j < 32; ++j) {
+      const int idj = __shfl_down_sync(0xffffffffu, id, j);
+      const long long cj = __shfl_down_sync(0xffffffffu, c, j);
+      if (more && lane + j < 32 && idj == id) {
+        sum += cj;
+      } else {
+        more = false;
+      }
+      if (!__any_sync(0xffffffffu, more)) break;
+    }
+    const unsigned heads = __ballot_sync(0xffffffffu, head);
+    const int nl = __popc(heads);
+    const int L = lk + lr;
+    long long new_off = 0;
+    if (lane == 0) {
+      const unsigned long long want = static_cast<unsigned long long>(L > 0 ? L : 1);
+      const unsigned long long at = atomicAdd(P.pool_top, want);
+      if (at + want > P.pool_cap) {
+        RaiseError(P.err, kErrPool, k, L, 0);
+        new_off = -1;
+      } else {
+        new_off = static_cast<long long>(at);
+      }
+    }
+    new_off = __shfl_sync(0xffffffffu, new_off, 0);
+    if (new_off < 0) continue;
+    if (head) Q.ent[new_off + __popc(heads & ((1u << lane) - 1u))] = MakeEnt(id, sum);
+    if (lane == 0) {
+      Q.internal[k] += Q.internal[r] + ekr;
+      Q.internal[r] = 0;
+      Q.size[k] += Q.size[r];
+      Q.size[r] = 0;
+      P.next[P.tail[k]] = P.head[r];
+      P.tail[k] = P.tail[r];
+      P.head[r] = -1;
+      P.fwd[r] = k;
+      Q.off[k] = new_off;
+      Q.len[k] = nl;
+      Q.cap[k] = L > 0 ? L : 1;
+      Q.len[r] = 0;
+      atomicAdd(&P.stats[kStAccepted], 1ull);
+      atomicAdd(&P.stats[kStTouched],
+                static_cast<unsigned long long>(2 + 3 * (lr - (ekr > 0 ? 1 : 0) - folded_sum)));
+      atomicAdd(&P.stats[kStUpdateBytes], 8ull * (2ull * L + nl));
+    }
   }
 }
 
@@ -2183,6 +2297,7 @@ __global__ void __launch_bounds__(kRowsThreads) RewriteRowsKernel(CommitParams P
     P.ctl->scratch_top = 0;
     P.ctl->short_cnt = 0;
     P.ctl->long_cnt = 0;
+    P.ctl->sel_total = 0;
     *P.ticket = 0u;
   }
 }
@@ -2433,6 +2548,10 @@ void Engine::LaunchCommit(int rg0, int nrg, int64_t max_pairs, bool verify) {
   C.rows_short = d_rows_short_.p;
   C.rows_long = d_rows_long_.p;
   C.ticket = d_rw_ticket_.p;
+  C.sel_list = d_sel_list_.p;
+  // warp-per-pair commit for short pairs, except in small blocks, where one
+  // launch is cheaper than a second one
+  C.warp_pairs = nrg > kFewGroups ? 1 : 0;
   if (verify) {
     const int vb = static_cast<int>(std::min<int64_t>((max_pairs + 7) / 8 + 1, 152 * 8));
     ++launches_;
@@ -2441,6 +2560,13 @@ void Engine::LaunchCommit(int rg0, int nrg, int64_t max_pairs, bool verify) {
   const int grid = static_cast<int>(std::min<int64_t>(std::max<int64_t>(max_pairs, 1), kRowsGrid));
   BeginTimed(kTimeUpdate);
   ++launches_;
+  // the warp kernel goes first: a pair it commits still reads as short to
+  // CommitKernel (its keep row can only be short), which skips it; a long
+  // pair is untouched until CommitKernel
+  if (C.warp_pairs) {
+    CommitShortKernel<<<static_cast<int>(std::min<int64_t>((max_pairs + 7) / 8 + 1, 152 * 8)), 256, 0, stream_>>>(C);
+    ++launches_;
+  }
   CommitKernel<<<grid, kRowsThreads, sizeof(RowsSmem), stream_>>>(C);
   ++launches_;
   RewriteRowsKernel<<<kRowsGrid, kRowsThreads, sizeof(RowsSmem), stream_>>>(C);
@@ -2610,6 +2736,7 @@ void Engine::RunBlock(size_t b, double threshold, int iter, int total_iterations
   LP.ctl = d_ctl_.p;
   LP.stats = d_stats_.p;
   LP.err = d_err_.p;
+  LP.sel_list = d_sel_list_.p;
   const int ss0 = h_block_sel_small_[b], ss1 = h_block_sel_small_[b + 1];
   const int sb0 = h_block_sel_big_[b], sb1 = h_block_sel_big_[b + 1];
   if (nrg <= kFewGroups) {
@@ -2817,7 +2944,7 @@ void Engine::MergePairs(const int32_t* keep, const int32_t* remove, int64_t coun
   CheckCuda(cudaMemsetAsync(d_ctl_.p, 0, sizeof(BlockCtl), stream_), "memset ctl");
   ++launches_;
   MarkKernel<<<(cnt + 255) / 256, 256, 0, stream_>>>(d_sel_keep_.p, d_sel_rem_.p, cnt, d_stamp_.p, d_partner_.p,
-                                                    d_seq_.p, block_stamp_);
+                                                    d_seq_.p, block_stamp_, d_sel_list_.p, d_ctl_.p);
   LaunchCommit(0, 1, count, false);
   ++launches_;
   RelabelKernel<<<(n_ + 255) / 256, 256, 0, stream_>>>(d_label_.p, d_fwd_.p, n_);

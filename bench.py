@@ -511,7 +511,12 @@ def main():
     ap.add_argument("--form", choices=list(FORMS), default="batched",
                     help="form whose throughput is the headline value")
     ap.add_argument("--no-other-form", action="store_true", help="skip timing the other forms")
+    ap.add_argument("--batch-groups", type=int, default=None,
+                    help="groups per block of the batched and ranker forms (default: all groups of an iteration)")
     args = ap.parse_args()
+    if args.batch_groups:
+        for f in ("batched", "ranker"):
+            FORMS[f]["group_batch_size"] = args.batch_groups
     if args.profile_run:
         profile_run(args)
         return
