@@ -218,7 +218,7 @@ class Engine {
   long long RankerExploreCap(long long slots) const;
   void RankerTrain();
   void RankerFinishIteration();
-  void LaunchPrepare(int s0, int s1, int b0, int b1, int t0, int t1);
+  void LaunchPrepare(int s0, int s1, int b0, int b1);
   void PrepareIterationBuffers();
   void BeginTimed(int which);
   void EndTimed(int which);
@@ -286,8 +286,6 @@ class Engine {
   std::vector<int> h_real_;      // Divide ids of the groups with >= 2 members
   std::vector<int> h_block_rg_;  // per 64-group block: first real-group position
   std::vector<int> h_small_, h_big_;              // real-group positions by prepare kernel
-  std::vector<int> h_tiny_, h_block_tiny_;        // tiny groups (own prepare instance) and per-block starts
-  DevBuf<int> d_tiny_;
   std::vector<int> h_block_small_, h_block_big_;  // per block: first entry in those lists
   DevBuf<int> d_small_, d_big_;
   std::vector<int> h_sel_small_, h_sel_mid_, h_sel_big_;  // real-group positions by select kernel

@@ -929,44 +929,35 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareOutputKernel(PrepareParam
 // the other lanes do the other pairs. Groups whose rows do not fit are handled
 // warp-cooperatively from global memory. Output and counters equal those of
 // PrepareKernel.
-// Two instances: groups of at most 32 members with at most 480 staged
-// entries (4 warps per CTA), and tiny groups of at most 8 members with at
-// most 256 entries (8 warps per CTA, a third of the shared memory per warp,
-// so more groups are resident per SM).
 constexpr int kSmallGroup = 32;
 constexpr int kSmallWarps = 4;
+constexpr int kSmallPairs = kSmallGroup * (kSmallGroup - 1) / 2;
 constexpr int kSmallStage = 480;  // staged row entries per group
-constexpr int kTinyGroup = 8;
-constexpr int kTinyWarps = 8;
-constexpr int kTinyStage = 256;
 
-template <int kG, int kStage>
 struct SmallWarpSmem {
-  long long p[kG * (kG - 1) / 2];  // upper triangle, TriIndex(a, b)
-  long long old[kG];
-  Entry ent[kStage];
-  int tsz[kStage];
-  int q[kG];
-  int sz[kG];
-  int len[kG];
-  int start[kG + 1];
-  unsigned fmask[kG];
-  long long off[kG];
+  long long p[kSmallPairs];  // upper triangle, TriIndex(a, b)
+  long long old[kSmallGroup];
+  Entry ent[kSmallStage];
+  int tsz[kSmallStage];
+  int q[kSmallGroup];
+  int sz[kSmallGroup];
+  int len[kSmallGroup];
+  int start[kSmallGroup + 1];
+  unsigned fmask[kSmallGroup];
+  long long off[kSmallGroup];
 };
 
-template <int kG, int kStage, int kWarps>
 struct SmallSmem {
-  SmallWarpSmem<kG, kStage> w[kWarps];
+  SmallWarpSmem w[kSmallWarps];
 };
 
 __device__ __forceinline__ int TriIndex(int a, int b, int g) { return a * (2 * g - a - 1) / 2 + (b - a - 1); }
 
-template <int kG, int kStage, int kWarps>
-__global__ void __launch_bounds__(kWarps * 32) PrepareSmallKernel(PrepareParams P) {
+__global__ void __launch_bounds__(kSmallWarps * 32) PrepareSmallKernel(PrepareParams P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmallWarpSmem<kG, kStage>& S = reinterpret_cast<SmallSmem<kG, kStage, kWarps>*>(smem_raw)->w[threadIdx.x >> 5];
+  SmallWarpSmem& S = reinterpret_cast<SmallSmem*>(smem_raw)->w[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
-  const int li = blockIdx.x * kWarps + (threadIdx.x >> 5);
+  const int li = blockIdx.x * kSmallWarps + (threadIdx.x >> 5);
   if (li >= P.nlist) return;
   const int ri = P.list[P.list0 + li];
   const int gid = P.real[ri];
@@ -996,7 +987,7 @@ __global__ void __launch_bounds__(kWarps * 32) PrepareSmallKernel(PrepareParams 
   if (lane == 0) S.start[g] = E;
   const int npairs = g * (g - 1) / 2;
   for (int k = lane; k < npairs; k += 32) S.p[k] = 0;
-  const bool staged = E <= kStage;
+  const bool staged = E <= kSmallStage;
   __syncwarp();
   if (staged) {
     // one flat pass over the group's entries (independent loads), then the
@@ -2332,14 +2323,8 @@ __global__ void RelabelKernel(int* __restrict__ label, const int* __restrict__ f
 void Engine::ConfigureKernels() {
   CheckCuda(cudaFuncSetAttribute(PrepareKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(sizeof(PrepSmem))), "prepare smem attribute");
-  CheckCuda(cudaFuncSetAttribute(PrepareSmallKernel<kSmallGroup, kSmallStage, kSmallWarps>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(sizeof(SmallSmem<kSmallGroup, kSmallStage, kSmallWarps>))),
-            "prepare-small smem attribute");
-  CheckCuda(cudaFuncSetAttribute(PrepareSmallKernel<kTinyGroup, kTinyStage, kTinyWarps>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(sizeof(SmallSmem<kTinyGroup, kTinyStage, kTinyWarps>))),
-            "prepare-tiny smem attribute");
+  CheckCuda(cudaFuncSetAttribute(PrepareSmallKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(sizeof(SmallSmem))), "prepare-small smem attribute");
   CheckCuda(cudaFuncSetAttribute(SelectMatchKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  8 * kMatchSmemKeys), "select smem attribute");
   CheckCuda(cudaFuncSetAttribute(CommitKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2380,8 +2365,6 @@ void Engine::PrepareIterationBuffers() {
   // go to the warp-per-group kernel; only the others need pair tables in
   // global memory
   h_small_.clear();
-  h_tiny_.clear();
-  h_block_tiny_.clear();
   h_big_.clear();
   h_big_moff_.assign(1, 0);
   h_soff_.assign(1, 0);
@@ -2393,7 +2376,6 @@ void Engine::PrepareIterationBuffers() {
   };
   for (size_t b = 0; b + 1 < h_block_rg_.size(); ++b) {
     h_block_small_.push_back(static_cast<int>(h_small_.size()));
-    h_block_tiny_.push_back(static_cast<int>(h_tiny_.size()));
     h_block_big_.push_back(static_cast<int>(h_big_.size()));
     // a small block with any big group sends all its groups to the big path
     // (one prepare path, fewer launches; the same candidates)
@@ -2401,9 +2383,6 @@ void Engine::PrepareIterationBuffers() {
     if (h_block_rg_[b + 1] - h_block_rg_[b] <= kFewGroups) {
       for (int ri = h_block_rg_[b]; ri < h_block_rg_[b + 1] && !all_big; ++ri) all_big = !is_small(ri);
     }
-    // tiny groups get their own kernel in large blocks (a second launch does
-    // not pay in a small block)
-    const bool tiny_ok = h_block_rg_[b + 1] - h_block_rg_[b] > kFewGroups;
     long long off = 0;
     for (int ri = h_block_rg_[b]; ri < h_block_rg_[b + 1]; ++ri) {
       const size_t gid = static_cast<size_t>(h_real_[static_cast<size_t>(ri)]);
@@ -2411,11 +2390,7 @@ void Engine::PrepareIterationBuffers() {
       // rows counted at Divide time (rows of supernodes not merged yet only
       // shrink during an iteration, so the count is an upper bound)
       if (!all_big && is_small(ri)) {
-        if (tiny_ok && g <= kTinyGroup && h_gent_[gid] <= static_cast<unsigned>(kTinyStage)) {
-          h_tiny_.push_back(ri);
-        } else {
-          h_small_.push_back(ri);
-        }
+        h_small_.push_back(ri);
         continue;
       }
       h_big_.push_back(ri);
@@ -2429,13 +2404,7 @@ void Engine::PrepareIterationBuffers() {
     max_mat = std::max(max_mat, off);
   }
   h_block_small_.push_back(static_cast<int>(h_small_.size()));
-  h_block_tiny_.push_back(static_cast<int>(h_tiny_.size()));
   h_block_big_.push_back(static_cast<int>(h_big_.size()));
-  d_tiny_.ensure(h_tiny_.size() + 1);
-  if (!h_tiny_.empty()) {
-    CheckCuda(cudaMemcpyAsync(d_tiny_.p, h_tiny_.data(), sizeof(int) * h_tiny_.size(), cudaMemcpyHostToDevice,
-                              stream_), "h2d tiny list");
-  }
   // selection: groups of at most kSelectSmallGroup members (at most 28
   // candidates) get one warp each, the others one CTA each
   h_sel_small_.clear();
@@ -2606,7 +2575,7 @@ void Engine::LaunchCommit(int rg0, int nrg, int64_t max_pairs, bool verify) {
 
 // EA-proxy candidates for the small-group list entries [s0, s1) (one warp
 // per group) and the big-group entries [b0, b1) (one CTA per group).
-void Engine::LaunchPrepare(int s0, int s1, int b0, int b1, int t0, int t1) {
+void Engine::LaunchPrepare(int s0, int s1, int b0, int b1) {
   PrepareParams PP;
   PP.Q = View();
   PP.order = d_order_.p;
@@ -2634,18 +2603,8 @@ void Engine::LaunchPrepare(int s0, int s1, int b0, int b1, int t0, int t1) {
     PP.list0 = s0;
     PP.nlist = s1 - s0;
     ++launches_;
-    PrepareSmallKernel<kSmallGroup, kSmallStage, kSmallWarps>
-        <<<(s1 - s0 + kSmallWarps - 1) / kSmallWarps, kSmallWarps * 32,
-           sizeof(SmallSmem<kSmallGroup, kSmallStage, kSmallWarps>), stream_>>>(PP);
-  }
-  if (t1 > t0) {
-    PP.list = d_tiny_.p;
-    PP.list0 = t0;
-    PP.nlist = t1 - t0;
-    ++launches_;
-    PrepareSmallKernel<kTinyGroup, kTinyStage, kTinyWarps>
-        <<<(t1 - t0 + kTinyWarps - 1) / kTinyWarps, kTinyWarps * 32,
-           sizeof(SmallSmem<kTinyGroup, kTinyStage, kTinyWarps>), stream_>>>(PP);
+    PrepareSmallKernel<<<(s1 - s0 + kSmallWarps - 1) / kSmallWarps, kSmallWarps * 32, sizeof(SmallSmem), stream_>>>(
+        PP);
   }
   if (b1 > b0) {
     PP.list = d_big_.p;
@@ -2703,8 +2662,7 @@ void Engine::RunBlock(size_t b, double threshold, int iter, int total_iterations
   const long long sel_slots = h_sel_off_[static_cast<size_t>(rg1)] - h_sel_off_[static_cast<size_t>(rg0)];
   // the block control words are zero: cleared by Merge before the first
   // block and by the previous block's rewrite kernel
-  LaunchPrepare(h_block_small_[b], h_block_small_[b + 1], h_block_big_[b], h_block_big_[b + 1], h_block_tiny_[b],
-                h_block_tiny_[b + 1]);
+  LaunchPrepare(h_block_small_[b], h_block_small_[b + 1], h_block_big_[b], h_block_big_[b + 1]);
   ScoreParams SP;
   SP.Q = View();
   SP.order = d_order_.p;
@@ -2925,8 +2883,7 @@ int64_t Engine::PrepareGroup(const int32_t* q, int g, int32_t* a_idx, int32_t* b
   ScatterGroupKernel<<<(g + 255) / 256, 256, 0, stream_>>>(dq.p, di.p, g, d_group_of_.p, d_idx_in_group_.p);
   PrepareIterationBuffers();
   CheckCuda(cudaMemsetAsync(d_ctl_.p, 0, sizeof(BlockCtl), stream_), "memset ctl");
-  LaunchPrepare(0, static_cast<int>(h_small_.size()), 0, static_cast<int>(h_big_.size()), 0,
-                static_cast<int>(h_tiny_.size()));
+  LaunchPrepare(0, static_cast<int>(h_small_.size()), 0, static_cast<int>(h_big_.size()));
   int cnt = 0;
   CheckCuda(cudaMemcpyAsync(&cnt, d_cand_cnt_.p, sizeof(int), cudaMemcpyDeviceToHost, stream_), "d2h");
   CheckCuda(cudaStreamSynchronize(stream_), "prepare sync");
