@@ -422,15 +422,20 @@ void Engine::Divide(int iter) {
                               cudaMemcpyDeviceToDevice, s), "copy glen");
   }
   n_groups_ = segs;
-  h_glen_.resize(static_cast<size_t>(segs));
-  h_gent_.resize(static_cast<size_t>(segs));
-  if (segs > 0) {
-    CheckCuda(cudaMemcpyAsync(h_glen_.data(), d_glen_.p, sizeof(int) * static_cast<size_t>(segs),
-                              cudaMemcpyDeviceToHost, s), "d2h glen");
-    CheckCuda(cudaMemcpyAsync(h_gent_.data(), d_gent_.p, sizeof(unsigned) * static_cast<size_t>(segs),
-                              cudaMemcpyDeviceToHost, s), "d2h gent");
+  // one block of every group: Merge plans the iteration on the device from
+  // d_glen_ / d_gent_, so nothing is read back here
+  plan_on_device_ = static_cast<long long>(cfg_.group_batch_size) >= static_cast<long long>(segs);
+  if (!plan_on_device_) {
+    h_glen_.resize(static_cast<size_t>(segs));
+    h_gent_.resize(static_cast<size_t>(segs));
+    if (segs > 0) {
+      CheckCuda(cudaMemcpyAsync(h_glen_.data(), d_glen_.p, sizeof(int) * static_cast<size_t>(segs),
+                                cudaMemcpyDeviceToHost, s), "d2h glen");
+      CheckCuda(cudaMemcpyAsync(h_gent_.data(), d_gent_.p, sizeof(unsigned) * static_cast<size_t>(segs),
+                                cudaMemcpyDeviceToHost, s), "d2h gent");
+    }
+    CheckCuda(cudaStreamSynchronize(s), "divide sync");
   }
-  CheckCuda(cudaStreamSynchronize(s), "divide sync");
   hstats_.groups_last = static_cast<uint64_t>(segs);
   hstats_.active_last = static_cast<uint64_t>(count);
 }

@@ -320,6 +320,10 @@ void Engine::EnsurePoolRoom() {
   CheckCuda(cudaMemcpyAsync(h_pin_.p, d_pool_top_.p, sizeof(top), cudaMemcpyDeviceToHost, stream_), "d2h pool top");
   CheckCuda(cudaStreamSynchronize(stream_), "sync");
   std::memcpy(&top, h_pin_.p, sizeof(top));
+  EnsurePoolRoom(top);
+}
+
+void Engine::EnsurePoolRoom(unsigned long long top) {
   // Keep rows of one iteration allocate at most the live entries plus one per
   // merge, so this much room guarantees no exhaustion inside the iteration.
   const size_t need = static_cast<size_t>(arcs_) + 2 * static_cast<size_t>(n_) + 1024;

@@ -140,6 +140,18 @@ struct BlockCtl {
   unsigned int pad;
 };
 
+// One block of an iteration's plan: its real-group range, its candidate and
+// selection slots, and the ranges of the prepare and select lists covering it.
+struct BlockPlan {
+  int rg0 = 0, rg1 = 0;                 // real-group positions
+  long long slots = 0, sel_slots = 0;   // candidate / selection slots
+  int s0 = 0, s1 = 0, b0 = 0, b1 = 0;   // small / big prepare list ranges
+  long long members = 0;                // members of the big groups
+  long long slot0 = 0, nslots = 0;      // sort slots of the deferred big groups
+  long long max_e = 0;                  // largest deferred group's row entries
+  int ss0 = 0, ss1 = 0, sm0 = 0, sm1 = 0, sb0 = 0, sb1 = 0;  // select list ranges
+};
+
 struct HostStats {
   double runtime_run_ms = 0, runtime_divide_ms = 0, runtime_merge_ms = 0;
   double merge_prepare_ms = 0, merge_score_ms = 0, merge_select_ms = 0, merge_update_ms = 0;
@@ -208,8 +220,9 @@ class Engine {
   void CheckError();
   void InitQuotient();
   void EnsurePoolRoom();
+  void EnsurePoolRoom(unsigned long long top);
   void CompactPool();
-  void RunBlock(size_t block, double threshold, int iter, int total_iterations);
+  void RunBlock(const BlockPlan& bp, double threshold, int iter, int total_iterations);
   void RankerReset();
   void RankerEnsure();
   void RankerLog(int rg0, int nrg, long long slots, int iter, double threshold, int total_iterations);
@@ -218,7 +231,9 @@ class Engine {
   long long RankerExploreCap(long long slots) const;
   void RankerTrain();
   void RankerFinishIteration();
-  void LaunchPrepare(int s0, int s1, int b0, int b1);
+  void LaunchPrepare(const BlockPlan& bp);
+  void PlanOnDevice();
+  void SizeIterationBuffers(size_t R, size_t ncand, size_t nsel, size_t nbig, long long max_mat, long long max_slots);
   void PrepareIterationBuffers();
   void BeginTimed(int which);
   void EndTimed(int which);
@@ -299,6 +314,10 @@ class Engine {
   DevBuf<long long> d_big_moff_;
   DevBuf<int> d_real_;
   std::vector<long long> h_cand_off_, h_sel_off_, h_mat_off_;
+  std::vector<BlockPlan> plans_;  // this iteration's blocks
+  bool plan_on_device_ = false;   // one-block iteration: Merge plans it on the device
+  DevBuf<unsigned char> d_plan_tiles_;
+  DevBuf<long long> d_plan_scalars_;
   PinnedBuf<long long> h_pin_;
   int block_stamp_ = 0;
   int64_t n_active_ = 0;

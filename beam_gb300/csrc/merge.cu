@@ -19,6 +19,7 @@
 // resulting rows are the canonical sorted, count-summed rows, identical to
 // the reference's sequential incremental updates.
 
+#include <cub/block/block_reduce.cuh>
 #include <cub/block/block_scan.cuh>
 #include <cub/device/device_radix_sort.cuh>
 
@@ -2337,6 +2338,206 @@ void Engine::ConfigureKernels() {
 // candidate / selection capacities (min(C(g,2), g*top_k) and g/2) as prefix
 // offsets, pair-table offsets restarting at every 64-group block, and for
 // every block the range of its real groups (empty blocks do no work).
+namespace {
+
+// ---- the plan of a one-block iteration, on the device ----
+// Per Divide group, the classification and offsets of the host plan
+// (PrepareIterationBuffers with one block of every group): tile sums, one
+// CTA scanning the tile sums, then every real group's entries scattered into
+// the lists in group order.
+constexpr int kPlanThreads = 256;
+constexpr int kPlanItems = 8;
+constexpr int kPlanTile = kPlanThreads * kPlanItems;
+enum PlanScalar : int {
+  kPlanR = 0, kPlanCand, kPlanSel, kPlanSmall, kPlanBig, kPlanMembers, kPlanSlots, kPlanMat, kPlanMaxE,
+  kPlanSelSmall, kPlanSelMid, kPlanSelBig, kPlanScalars
+};
+
+struct PlanSums {
+  long long cand, sel, moff, soff, mat;
+  int real, small, big, ssmall, smid, sbig;
+};
+
+struct PlanSumOp {
+  __device__ __forceinline__ PlanSums operator()(const PlanSums& a, const PlanSums& b) const {
+    PlanSums r;
+    r.cand = a.cand + b.cand;
+    r.sel = a.sel + b.sel;
+    r.moff = a.moff + b.moff;
+    r.soff = a.soff + b.soff;
+    r.mat = a.mat + b.mat;
+    r.real = a.real + b.real;
+    r.small = a.small + b.small;
+    r.big = a.big + b.big;
+    r.ssmall = a.ssmall + b.ssmall;
+    r.smid = a.smid + b.smid;
+    r.sbig = a.sbig + b.sbig;
+    return r;
+  }
+};
+
+__device__ __forceinline__ PlanSums PlanZero() {
+  PlanSums z;
+  z.cand = z.sel = z.moff = z.soff = z.mat = 0;
+  z.real = z.small = z.big = z.ssmall = z.smid = z.sbig = 0;
+  return z;
+}
+
+// one group's contribution: the same rules as the host plan
+__device__ __forceinline__ PlanSums PlanOfGroup(int g, unsigned e, long long k) {
+  PlanSums f = PlanZero();
+  if (g < 2) return f;
+  const long long gl = g;
+  f.real = 1;
+  f.cand = gl * (gl - 1) / 2 < gl * k ? gl * (gl - 1) / 2 : gl * k;
+  f.sel = gl / 2;
+  if (g <= kSmallGroup && e <= static_cast<unsigned>(kSmallStage)) {
+    f.small = 1;
+  } else {
+    f.big = 1;
+    f.moff = gl;
+    f.soff = e > static_cast<unsigned>(kSmemEntries) ? static_cast<long long>(e) : 0;
+    f.mat = (OldCostOffset(gl * gl) + 8 * gl + 255) & ~255ll;
+  }
+  if (g <= kSelectSmallGroup) {
+    f.ssmall = 1;
+  } else if (g <= kSelectMidGroup) {
+    f.smid = 1;
+  } else {
+    f.sbig = 1;
+  }
+  return f;
+}
+
+struct PlanParams {
+  const int* glen;
+  const unsigned* gent;
+  long long G;
+  long long top_k;
+  PlanSums* tile_sums;
+  PlanSums* tile_off;
+  int tiles;
+  long long* scalars;
+  int* real;
+  long long* cand_off;
+  long long* sel_off;
+  long long* mat_off;
+  int* small;
+  int* big;
+  long long* big_moff;
+  long long* soff;
+  int* sel_small;
+  int* sel_mid;
+  int* sel_big;
+};
+
+__global__ void __launch_bounds__(kPlanThreads) PlanTileKernel(PlanParams P) {
+  using Reduce = cub::BlockReduce<PlanSums, kPlanThreads>;
+  __shared__ typename Reduce::TempStorage tmp;
+  const long long base = static_cast<long long>(blockIdx.x) * kPlanTile + threadIdx.x * kPlanItems;
+  PlanSums acc = PlanZero();
+  long long max_e = 0;
+  for (int j = 0; j < kPlanItems; ++j) {
+    const long long gi = base + j;
+    if (gi >= P.G) break;
+    const PlanSums f = PlanOfGroup(P.glen[gi], P.gent[gi], P.top_k);
+    acc = PlanSumOp()(acc, f);
+    max_e = f.soff > max_e ? f.soff : max_e;
+  }
+  const PlanSums t = Reduce(tmp).Reduce(acc, PlanSumOp());
+  if (threadIdx.x == 0) P.tile_sums[blockIdx.x] = t;
+  if (max_e > 0) {
+    atomicMax(reinterpret_cast<unsigned long long*>(P.scalars + kPlanMaxE), static_cast<unsigned long long>(max_e));
+  }
+}
+
+// one CTA: exclusive offsets of the tiles, the totals, and the closing
+// entries of the offset arrays
+__global__ void __launch_bounds__(kPlanThreads) PlanScanKernel(PlanParams P) {
+  using Scan = cub::BlockScan<PlanSums, kPlanThreads>;
+  __shared__ typename Scan::TempStorage tmp;
+  __shared__ PlanSums carry;
+  if (threadIdx.x == 0) carry = PlanZero();
+  __syncthreads();
+  for (int t0 = 0; t0 < P.tiles; t0 += kPlanThreads) {
+    const int t = t0 + threadIdx.x;
+    const PlanSums v = t < P.tiles ? P.tile_sums[t] : PlanZero();
+    PlanSums ex, total;
+    Scan(tmp).ExclusiveScan(v, ex, PlanZero(), PlanSumOp(), total);
+    const PlanSums c = carry;
+    if (t < P.tiles) P.tile_off[t] = PlanSumOp()(c, ex);
+    __syncthreads();
+    if (threadIdx.x == 0) carry = PlanSumOp()(c, total);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const PlanSums T = carry;
+    long long* s = P.scalars;
+    s[kPlanR] = T.real;
+    s[kPlanCand] = T.cand;
+    s[kPlanSel] = T.sel;
+    s[kPlanSmall] = T.small;
+    s[kPlanBig] = T.big;
+    s[kPlanMembers] = T.moff;
+    s[kPlanSlots] = T.soff;
+    s[kPlanMat] = T.mat;
+    s[kPlanSelSmall] = T.ssmall;
+    s[kPlanSelMid] = T.smid;
+    s[kPlanSelBig] = T.sbig;
+    P.cand_off[T.real] = T.cand;
+    P.sel_off[T.real] = T.sel;
+    P.mat_off[T.real] = 0;
+    P.big_moff[T.big] = T.moff;
+    P.soff[T.big] = T.soff;
+  }
+}
+
+__global__ void __launch_bounds__(kPlanThreads) PlanScatterKernel(PlanParams P) {
+  using Scan = cub::BlockScan<PlanSums, kPlanThreads>;
+  __shared__ typename Scan::TempStorage tmp;
+  const long long base = static_cast<long long>(blockIdx.x) * kPlanTile + threadIdx.x * kPlanItems;
+  int g[kPlanItems];
+  unsigned e[kPlanItems];
+  PlanSums acc = PlanZero();
+#pragma unroll
+  for (int j = 0; j < kPlanItems; ++j) {
+    const long long gi = base + j;
+    g[j] = gi < P.G ? P.glen[gi] : 0;
+    e[j] = gi < P.G ? P.gent[gi] : 0u;
+    acc = PlanSumOp()(acc, PlanOfGroup(g[j], e[j], P.top_k));
+  }
+  PlanSums off;
+  Scan(tmp).ExclusiveScan(acc, off, P.tile_off[blockIdx.x], PlanSumOp());
+#pragma unroll
+  for (int j = 0; j < kPlanItems; ++j) {
+    const PlanSums f = PlanOfGroup(g[j], e[j], P.top_k);
+    if (f.real) {
+      const int ri = off.real;
+      P.real[ri] = static_cast<int>(base + j);
+      P.cand_off[ri] = off.cand;
+      P.sel_off[ri] = off.sel;
+      P.mat_off[ri] = f.big ? off.mat : 0;
+      if (f.small) {
+        P.small[off.small] = ri;
+      } else {
+        P.big[off.big] = ri;
+        P.big_moff[off.big] = off.moff;
+        P.soff[off.big] = off.soff;
+      }
+      if (f.ssmall) {
+        P.sel_small[off.ssmall] = ri;
+      } else if (f.smid) {
+        P.sel_mid[off.smid] = ri;
+      } else {
+        P.sel_big[off.sbig] = ri;
+      }
+    }
+    off = PlanSumOp()(off, f);
+  }
+}
+
+}  // namespace
+
 void Engine::PrepareIterationBuffers() {
   const int64_t G = n_groups_;
   h_real_.clear();
@@ -2442,22 +2643,10 @@ void Engine::PrepareIterationBuffers() {
   }
   d_small_.ensure(h_small_.size() + 1);
   d_big_.ensure(h_big_.size() + 1);
-  d_bigdesc_.ensure(sizeof(BigDesc) * (h_big_.size() + 1));
   long long max_slots = 1;
   for (size_t b = 0; b + 1 < h_block_big_.size(); ++b) {
     max_slots = std::max(max_slots, h_soff_[static_cast<size_t>(h_block_big_[b + 1])] -
                                         h_soff_[static_cast<size_t>(h_block_big_[b])]);
-  }
-  for (int k = 0; k < 2; ++k) {
-    d_skey_[k].ensure(static_cast<size_t>(max_slots));
-    d_sval_[k].ensure(static_cast<size_t>(max_slots));
-  }
-  // radix-sort scratch of the deferred groups, sized once per iteration
-  if (max_slots > 1) {
-    size_t bytes = 0;
-    CheckCuda(cub::DeviceRadixSort::SortPairs(nullptr, bytes, d_skey_[0].p, d_skey_[1].p, d_sval_[0].p,
-                                              d_sval_[1].p, max_slots, 0, 64, stream_), "cub radix sort size");
-    d_cub_tmp_.ensure(bytes);
   }
   d_soff_.ensure(h_soff_.size());
   CheckCuda(cudaMemcpyAsync(d_soff_.p, h_soff_.data(), sizeof(long long) * h_soff_.size(), cudaMemcpyHostToDevice,
@@ -2477,9 +2666,63 @@ void Engine::PrepareIterationBuffers() {
   d_cand_off_.ensure(R + 1);
   d_sel_off_.ensure(R + 1);
   d_mat_off_.ensure(R + 1);
+  if (R > 0) {
+    CheckCuda(cudaMemcpyAsync(d_real_.p, h_real_.data(), sizeof(int) * R, cudaMemcpyHostToDevice, stream_),
+              "h2d real");
+    CheckCuda(cudaMemcpyAsync(d_cand_off_.p, h_cand_off_.data(), sizeof(long long) * (R + 1),
+                              cudaMemcpyHostToDevice, stream_), "h2d cand_off");
+    CheckCuda(cudaMemcpyAsync(d_sel_off_.p, h_sel_off_.data(), sizeof(long long) * (R + 1),
+                              cudaMemcpyHostToDevice, stream_), "h2d sel_off");
+    CheckCuda(cudaMemcpyAsync(d_mat_off_.p, h_mat_off_.data(), sizeof(long long) * (R + 1),
+                              cudaMemcpyHostToDevice, stream_), "h2d mat_off");
+  }
+  SizeIterationBuffers(R, static_cast<size_t>(h_cand_off_[R]), static_cast<size_t>(h_sel_off_[R]), h_big_.size(),
+                       max_mat, max_slots);
+  plans_.clear();
+  for (size_t b = 0; b + 1 < h_block_rg_.size(); ++b) {
+    BlockPlan bp;
+    bp.rg0 = h_block_rg_[b];
+    bp.rg1 = h_block_rg_[b + 1];
+    bp.slots = h_cand_off_[static_cast<size_t>(bp.rg1)] - h_cand_off_[static_cast<size_t>(bp.rg0)];
+    bp.sel_slots = h_sel_off_[static_cast<size_t>(bp.rg1)] - h_sel_off_[static_cast<size_t>(bp.rg0)];
+    bp.s0 = h_block_small_[b];
+    bp.s1 = h_block_small_[b + 1];
+    bp.b0 = h_block_big_[b];
+    bp.b1 = h_block_big_[b + 1];
+    bp.members = h_big_moff_[static_cast<size_t>(bp.b1)] - h_big_moff_[static_cast<size_t>(bp.b0)];
+    bp.slot0 = h_soff_[static_cast<size_t>(bp.b0)];
+    bp.nslots = h_soff_[static_cast<size_t>(bp.b1)] - bp.slot0;
+    for (int i = bp.b0; i < bp.b1; ++i) {
+      bp.max_e = std::max(bp.max_e, h_soff_[static_cast<size_t>(i) + 1] - h_soff_[static_cast<size_t>(i)]);
+    }
+    bp.ss0 = h_block_sel_small_[b];
+    bp.ss1 = h_block_sel_small_[b + 1];
+    bp.sm0 = h_block_sel_mid_[b];
+    bp.sm1 = h_block_sel_mid_[b + 1];
+    bp.sb0 = h_block_sel_big_[b];
+    bp.sb1 = h_block_sel_big_[b + 1];
+    plans_.push_back(bp);
+  }
+}
+
+// Buffers whose sizes follow from the plan's totals (either planner).
+void Engine::SizeIterationBuffers(size_t R, size_t ncand, size_t nsel, size_t nbig, long long max_mat,
+                                  long long max_slots) {
+  d_bigdesc_.ensure(sizeof(BigDesc) * (nbig + 1));
+  max_slots = std::max(max_slots, 1ll);
+  for (int k = 0; k < 2; ++k) {
+    d_skey_[k].ensure(static_cast<size_t>(max_slots));
+    d_sval_[k].ensure(static_cast<size_t>(max_slots));
+  }
+  // radix-sort scratch of the deferred groups, sized once per iteration
+  if (max_slots > 1) {
+    size_t bytes = 0;
+    CheckCuda(cub::DeviceRadixSort::SortPairs(nullptr, bytes, d_skey_[0].p, d_skey_[1].p, d_sval_[0].p,
+                                              d_sval_[1].p, max_slots, 0, 64, stream_), "cub radix sort size");
+    d_cub_tmp_.ensure(bytes);
+  }
   d_cand_cnt_.ensure(R + 1);
   d_sel_cnt_.ensure(R + 1);
-  const size_t ncand = static_cast<size_t>(h_cand_off_[R]);
   d_cand_.ensure(ncand + 1);
   d_cand_rep_.ensure(ncand + 1);
   CheckCuda(cudaMemsetAsync(d_cand_rep_.p, 0xff, sizeof(int2) * (ncand + 1), stream_), "memset cand reps");
@@ -2491,21 +2734,80 @@ void Engine::PrepareIterationBuffers() {
     for (int k = 0; k < 2; ++k) d_rk_zpos_[k].ensure(static_cast<size_t>(RankerExploreCap(static_cast<long long>(ncand))));
   }
   rk_iter_slots_ = static_cast<long long>(ncand);
-  const size_t nsel = static_cast<size_t>(h_sel_off_[R]);
   d_sel_keep_.ensure(nsel + 1);
   d_sel_rem_.ensure(nsel + 1);
   d_sel_gain_.ensure(nsel + 1);
   d_mat_.ensure(static_cast<size_t>(max_mat) + 256);
-  if (R > 0) {
-    CheckCuda(cudaMemcpyAsync(d_real_.p, h_real_.data(), sizeof(int) * R, cudaMemcpyHostToDevice, stream_),
-              "h2d real");
-    CheckCuda(cudaMemcpyAsync(d_cand_off_.p, h_cand_off_.data(), sizeof(long long) * (R + 1),
-                              cudaMemcpyHostToDevice, stream_), "h2d cand_off");
-    CheckCuda(cudaMemcpyAsync(d_sel_off_.p, h_sel_off_.data(), sizeof(long long) * (R + 1),
-                              cudaMemcpyHostToDevice, stream_), "h2d sel_off");
-    CheckCuda(cudaMemcpyAsync(d_mat_off_.p, h_mat_off_.data(), sizeof(long long) * (R + 1),
-                              cudaMemcpyHostToDevice, stream_), "h2d mat_off");
+}
+
+// The plan of a one-block iteration, made on the device from the Divide
+// output (the same lists and offsets as PrepareIterationBuffers); one small
+// read-back brings the totals and the entry-pool top to the host.
+void Engine::PlanOnDevice() {
+  const long long G = n_groups_;
+  const size_t cap = static_cast<size_t>(G) + 1;
+  for (DevBuf<int>* b : {&d_real_, &d_small_, &d_big_, &d_sel_small_, &d_sel_mid_, &d_sel_big_}) b->ensure(cap);
+  for (DevBuf<long long>* b : {&d_cand_off_, &d_sel_off_, &d_mat_off_, &d_big_moff_, &d_soff_}) b->ensure(cap);
+  const int tiles = static_cast<int>((G + kPlanTile - 1) / kPlanTile);
+  d_plan_tiles_.ensure(sizeof(PlanSums) * (2 * static_cast<size_t>(tiles) + 1));
+  d_plan_scalars_.ensure(kPlanScalars);
+  CheckCuda(cudaMemsetAsync(d_plan_scalars_.p, 0, sizeof(long long) * kPlanScalars, stream_), "memset plan");
+  PlanParams P;
+  P.glen = d_glen_.p;
+  P.gent = d_gent_.p;
+  P.G = G;
+  P.top_k = cfg_.top_k > 0 ? cfg_.top_k : 1;
+  P.tile_sums = reinterpret_cast<PlanSums*>(d_plan_tiles_.p);
+  P.tile_off = P.tile_sums + tiles;
+  P.tiles = tiles;
+  P.scalars = d_plan_scalars_.p;
+  P.real = d_real_.p;
+  P.cand_off = d_cand_off_.p;
+  P.sel_off = d_sel_off_.p;
+  P.mat_off = d_mat_off_.p;
+  P.small = d_small_.p;
+  P.big = d_big_.p;
+  P.big_moff = d_big_moff_.p;
+  P.soff = d_soff_.p;
+  P.sel_small = d_sel_small_.p;
+  P.sel_mid = d_sel_mid_.p;
+  P.sel_big = d_sel_big_.p;
+  if (tiles > 0) {
+    ++launches_;
+    PlanTileKernel<<<tiles, kPlanThreads, 0, stream_>>>(P);
   }
+  ++launches_;
+  PlanScanKernel<<<1, kPlanThreads, 0, stream_>>>(P);
+  if (tiles > 0) {
+    ++launches_;
+    PlanScatterKernel<<<tiles, kPlanThreads, 0, stream_>>>(P);
+  }
+  long long* hs = h_pin_.p + 16;
+  CheckCuda(cudaMemcpyAsync(hs, d_plan_scalars_.p, sizeof(long long) * kPlanScalars, cudaMemcpyDeviceToHost,
+                            stream_), "d2h plan");
+  CheckCuda(cudaMemcpyAsync(hs + kPlanScalars, d_pool_top_.p, sizeof(long long), cudaMemcpyDeviceToHost, stream_),
+            "d2h pool top");
+  CheckCuda(cudaStreamSynchronize(stream_), "plan sync");
+  CheckError();
+  long long v[kPlanScalars + 1];
+  std::memcpy(v, hs, sizeof(v));
+  EnsurePoolRoom(static_cast<unsigned long long>(v[kPlanScalars]));
+  const size_t R = static_cast<size_t>(v[kPlanR]);
+  SizeIterationBuffers(R, static_cast<size_t>(v[kPlanCand]), static_cast<size_t>(v[kPlanSel]),
+                       static_cast<size_t>(v[kPlanBig]), v[kPlanMat], v[kPlanSlots]);
+  BlockPlan bp;
+  bp.rg1 = static_cast<int>(R);
+  bp.slots = v[kPlanCand];
+  bp.sel_slots = v[kPlanSel];
+  bp.s1 = static_cast<int>(v[kPlanSmall]);
+  bp.b1 = static_cast<int>(v[kPlanBig]);
+  bp.members = v[kPlanMembers];
+  bp.nslots = v[kPlanSlots];
+  bp.max_e = v[kPlanMaxE];
+  bp.ss1 = static_cast<int>(v[kPlanSelSmall]);
+  bp.sm1 = static_cast<int>(v[kPlanSelMid]);
+  bp.sb1 = static_cast<int>(v[kPlanSelBig]);
+  plans_.assign(1, bp);
 }
 
 QuotientView Engine::View() {
@@ -2575,7 +2877,8 @@ void Engine::LaunchCommit(int rg0, int nrg, int64_t max_pairs, bool verify) {
 
 // EA-proxy candidates for the small-group list entries [s0, s1) (one warp
 // per group) and the big-group entries [b0, b1) (one CTA per group).
-void Engine::LaunchPrepare(int s0, int s1, int b0, int b1) {
+void Engine::LaunchPrepare(const BlockPlan& bp) {
+  const int s0 = bp.s0, s1 = bp.s1, b0 = bp.b0, b1 = bp.b1;
   PrepareParams PP;
   PP.Q = View();
   PP.order = d_order_.p;
@@ -2611,21 +2914,18 @@ void Engine::LaunchPrepare(int s0, int s1, int b0, int b1) {
     PP.list0 = b0;
     PP.nlist = b1 - b0;
     PP.moff = d_big_moff_.p;
-    const long long members = h_big_moff_[static_cast<size_t>(b1)] - h_big_moff_[static_cast<size_t>(b0)];
+    const long long members = bp.members;
     PP.desc = reinterpret_cast<BigDesc*>(d_bigdesc_.p);
     PP.soff = d_soff_.p;
-    PP.slot0 = h_soff_[static_cast<size_t>(b0)];
-    PP.nslots = h_soff_[static_cast<size_t>(b1)] - PP.slot0;
+    PP.slot0 = bp.slot0;
+    PP.nslots = bp.nslots;
     PP.skey = d_skey_[0].p;
     PP.sval = d_sval_[0].p;
     PP.skey_sorted = d_skey_[1].p;
     PP.sval_sorted = d_sval_[1].p;
     // slices per deferred group: about 2048 row entries per CTA of the
     // largest group (row totals as counted at Divide time)
-    long long max_e = 0;
-    for (int b = b0; b < b1; ++b) {
-      max_e = std::max(max_e, h_soff_[static_cast<size_t>(b) + 1] - h_soff_[static_cast<size_t>(b)]);
-    }
+    const long long max_e = bp.max_e;
     ++launches_;
     PrepareKernel<<<b1 - b0, kPrepThreads, sizeof(PrepSmem), stream_>>>(PP);
     if (PP.nslots > 0) {
@@ -2652,17 +2952,16 @@ void Engine::LaunchPrepare(int s0, int s1, int b0, int b1) {
   EndTimed(kTimePrepare);
 }
 
-void Engine::RunBlock(size_t b, double threshold, int iter, int total_iterations) {
+void Engine::RunBlock(const BlockPlan& bp, double threshold, int iter, int total_iterations) {
   ++block_stamp_;
   ++hstats_.blocks;
-  const int rg0 = h_block_rg_[b];
-  const int rg1 = h_block_rg_[b + 1];
-  const int nrg = rg1 - rg0;
-  const long long slots = h_cand_off_[static_cast<size_t>(rg1)] - h_cand_off_[static_cast<size_t>(rg0)];
-  const long long sel_slots = h_sel_off_[static_cast<size_t>(rg1)] - h_sel_off_[static_cast<size_t>(rg0)];
+  const int rg0 = bp.rg0;
+  const int nrg = bp.rg1 - bp.rg0;
+  const long long slots = bp.slots;
+  const long long sel_slots = bp.sel_slots;
   // the block control words are zero: cleared by Merge before the first
   // block and by the previous block's rewrite kernel
-  LaunchPrepare(h_block_small_[b], h_block_small_[b + 1], h_block_big_[b], h_block_big_[b + 1]);
+  LaunchPrepare(bp);
   ScoreParams SP;
   SP.Q = View();
   SP.order = d_order_.p;
@@ -2737,8 +3036,8 @@ void Engine::RunBlock(size_t b, double threshold, int iter, int total_iterations
   LP.stats = d_stats_.p;
   LP.err = d_err_.p;
   LP.sel_list = d_sel_list_.p;
-  const int ss0 = h_block_sel_small_[b], ss1 = h_block_sel_small_[b + 1];
-  const int sb0 = h_block_sel_big_[b], sb1 = h_block_sel_big_[b + 1];
+  const int ss0 = bp.ss0, ss1 = bp.ss1;
+  const int sb0 = bp.sb0, sb1 = bp.sb1;
   if (nrg <= kFewGroups) {
     // a small block: one launch, a CTA per group (same selection)
     LP.list = nullptr;
@@ -2757,7 +3056,7 @@ void Engine::RunBlock(size_t b, double threshold, int iter, int total_iterations
     SelectSmallKernel<<<(ss1 - ss0 + kSelectSmallWarps - 1) / kSelectSmallWarps, kSelectSmallWarps * 32, 0,
                         stream_>>>(LP);
   }
-  const int sm0 = h_block_sel_mid_[b], sm1 = h_block_sel_mid_[b + 1];
+  const int sm0 = bp.sm0, sm1 = bp.sm1;
   if (sm1 > sm0) {
     LP.list = d_sel_mid_.p;
     LP.list0 = sm0;
@@ -2780,11 +3079,15 @@ void Engine::Merge(int iter, int total_iterations) {
   if (n_groups_ < 0) throw std::runtime_error("Merge requires a preceding Divide");
   // ComputeMergeThreshold, reciprocal policy (src/sweg.cpp:400-406)
   const double threshold = 1.0 / static_cast<double>(iter + 1);
-  EnsurePoolRoom();
-  PrepareIterationBuffers();
+  if (plan_on_device_) {
+    PlanOnDevice();
+  } else {
+    EnsurePoolRoom();
+    PrepareIterationBuffers();
+  }
   CheckCuda(cudaMemsetAsync(d_ctl_.p, 0, sizeof(BlockCtl), stream_), "memset ctl");
-  for (size_t b = 0; b + 1 < h_block_rg_.size(); ++b) {
-    if (h_block_rg_[b + 1] > h_block_rg_[b]) RunBlock(b, threshold, iter, total_iterations);
+  for (const BlockPlan& bp : plans_) {
+    if (bp.rg1 > bp.rg0) RunBlock(bp, threshold, iter, total_iterations);
   }
   ++launches_;
   RelabelKernel<<<(n_ + 255) / 256, 256, 0, stream_>>>(d_label_.p, d_fwd_.p, n_);
@@ -2883,7 +3186,7 @@ int64_t Engine::PrepareGroup(const int32_t* q, int g, int32_t* a_idx, int32_t* b
   ScatterGroupKernel<<<(g + 255) / 256, 256, 0, stream_>>>(dq.p, di.p, g, d_group_of_.p, d_idx_in_group_.p);
   PrepareIterationBuffers();
   CheckCuda(cudaMemsetAsync(d_ctl_.p, 0, sizeof(BlockCtl), stream_), "memset ctl");
-  LaunchPrepare(0, static_cast<int>(h_small_.size()), 0, static_cast<int>(h_big_.size()));
+  LaunchPrepare(plans_.at(0));
   int cnt = 0;
   CheckCuda(cudaMemcpyAsync(&cnt, d_cand_cnt_.p, sizeof(int), cudaMemcpyDeviceToHost, stream_), "d2h");
   CheckCuda(cudaStreamSynchronize(stream_), "prepare sync");
