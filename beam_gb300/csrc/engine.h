@@ -149,6 +149,7 @@ struct BlockPlan {
   long long members = 0;                // members of the big groups
   long long slot0 = 0, nslots = 0;      // sort slots of the deferred big groups
   long long max_e = 0;                  // largest deferred group's row entries
+  long long mat_bytes = 0;              // pair tables of the big groups
   int ss0 = 0, ss1 = 0, sm0 = 0, sm1 = 0, sb0 = 0, sb1 = 0;  // select list ranges
 };
 

@@ -35,6 +35,11 @@ constexpr int kPrepThreads = 512;
 constexpr int kLaneTopK = 32;        // per-lane candidate lists for top_k up to this
 constexpr int kSmemEntries = 2048;   // bucket entries held in shared memory
 constexpr int kSmemHeads = 4096;     // bucket hash heads in shared memory
+// Groups of more than this many members take the sorted (GPU-wide) path
+// even when their rows fit the shared-memory table: the pairs of members
+// sharing a target grow with the square of the member count, too much work
+// for one CTA.
+constexpr int kSmemMaxGroup = 64;
 constexpr int kScoreThreads = 256;
 constexpr int kFewGroups = 256;  // blocks of at most this many groups take fewer, wider launches
 constexpr int kSelectMidGroup = 32;   // groups of 9..32 members: a small CTA each
@@ -235,6 +240,7 @@ struct PrepareParams {
   int* cand_cnt;
   const long long* mat_off;
   unsigned char* mat;
+  int mat_zeroed;  // the pair tables were cleared by one memset of the block
   unsigned char* scratch;
   unsigned long long scratch_cap;
   BlockCtl* ctl;
@@ -383,9 +389,11 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
       old_out[i] = internal > 0 ? EncodeCostForPair(S.q[i], si, S.q[i], si, 2 * internal) : 0;
     }
     if (tid == 0) V.eoff[g] = E;
-    for (long long k = tid; k < gg; k += kPrepThreads) {
-      pmat[k] = 0;
-      fmat[k] = 0;
+    if (!P.mat_zeroed) {
+      for (long long k = tid; k < gg; k += kPrepThreads) {
+        pmat[k] = 0;
+        fmat[k] = 0;
+      }
     }
     if (tid == 0) {
       desc->base = dbase;
@@ -413,9 +421,11 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
   const unsigned hmask = kSmemHeads - 1;
   for (unsigned h = tid; h <= hmask; h += kPrepThreads) heads[h] = -1;
   // per-group tables: proxy int64[g*g] | kept flag u8[g*g] | old cost int64[g]
-  for (long long k = tid; k < gg; k += kPrepThreads) {
-    pmat[k] = 0;
-    fmat[k] = 0;
+  if (!P.mat_zeroed) {
+    for (long long k = tid; k < gg; k += kPrepThreads) {
+      pmat[k] = 0;
+      fmat[k] = 0;
+    }
   }
   __syncthreads();
   // entries, approximate old costs and direct in-group edges
@@ -560,52 +570,112 @@ __global__ void __launch_bounds__(kFillThreads) PrepareFillKernel(PrepareParams 
   }
 }
 
-// Accumulate pass of the deferred groups over the sorted slots: the entries
-// of one (group, target) are a contiguous run; the thread at run position p
-// pairs its member with the members at positions before p in the run, so each
-// member pair sharing a target is visited once, and adds
-// proxy += max(0, old - new) to both halves of the pair table.
+// Accumulate pass of the deferred groups over the sorted slots, a warp per
+// 32 consecutive slots. The entries of one (group, target) are a contiguous
+// run; each lane pairs its entry with the earlier entries of its run: those
+// in its own chunk by shuffles, and, for the run that reaches back past the
+// chunk's start, those of the earlier chunks, 32 at a time. Every member pair
+// sharing a target is visited once and adds proxy += max(0, old - new) to
+// both halves of the pair table.
+struct RunEntry {
+  unsigned long long key;
+  long long c, s;  // edge count to the target, member size
+  int i, q;        // member index, member supernode
+};
+
+__device__ __forceinline__ RunEntry LoadRunEntry(const PrepareParams& P, long long p, const DeferredView& V) {
+  RunEntry r;
+  const unsigned long long v = P.sval_sorted[p];
+  r.i = static_cast<int>(v >> 32);
+  r.c = static_cast<long long>(v & 0xffffffffu);
+  r.s = V.msz[r.i];
+  r.q = V.mq[r.i];
+  return r;
+}
+
+__device__ __forceinline__ RunEntry ShflRunEntry(const RunEntry& r, int src) {
+  RunEntry o;
+  o.key = __shfl_sync(0xffffffffu, r.key, src);
+  o.c = __shfl_sync(0xffffffffu, r.c, src);
+  o.s = __shfl_sync(0xffffffffu, r.s, src);
+  o.i = __shfl_sync(0xffffffffu, r.i, src);
+  o.q = __shfl_sync(0xffffffffu, r.q, src);
+  return o;
+}
+
+__device__ __forceinline__ void AccumPair(const RunEntry& a, const RunEntry& b, int t, long long st, int g,
+                                          long long* pmat, unsigned long long& examined) {
+  ++examined;
+  const long long oldc = EncodeCostForPair(a.q, a.s, t, st, a.c) + EncodeCostForPair(b.q, b.s, t, st, b.c);
+  const long long newc = EncodeCostForPair(a.q, a.s + b.s, t, st, a.c + b.c);
+  const long long delta = oldc - newc;
+  if (delta > 0) {
+    atomicAdd(reinterpret_cast<unsigned long long*>(&pmat[static_cast<long long>(a.i) * g + b.i]),
+              static_cast<unsigned long long>(delta));
+    atomicAdd(reinterpret_cast<unsigned long long*>(&pmat[static_cast<long long>(b.i) * g + a.i]),
+              static_cast<unsigned long long>(delta));
+  }
+}
+
 __global__ void __launch_bounds__(kAccumThreads) PrepareAccumKernel(PrepareParams P) {
+  const int lane = threadIdx.x & 31;
   unsigned long long examined = 0;
-  const long long stride = static_cast<long long>(gridDim.x) * kAccumThreads;
-  for (long long p = static_cast<long long>(blockIdx.x) * kAccumThreads + threadIdx.x; p < P.nslots; p += stride) {
-    const unsigned long long key = P.skey_sorted[p];
-    if (key == kSlotPad) continue;
-    if (p == 0 || P.skey_sorted[p - 1] != key) continue;  // run head: no earlier entry
-    const int bl = static_cast<int>(key >> 32);
-    const int t = static_cast<int>(key & 0xffffffffu);
-    if (bl >= P.nlist) continue;
-    const BigDesc d = P.desc[P.list0 + bl];
-    const int ri = P.list[P.list0 + bl];
-    const int g = P.glen[P.real[ri]];
-    long long* pmat = reinterpret_cast<long long*>(P.mat + P.mat_off[ri]);
-    const DeferredView V = Deferred(d.base, g);
-    const unsigned long long vi = P.sval_sorted[p];
-    const int i = static_cast<int>(vi >> 32);
-    const long long c = static_cast<long long>(vi & 0xffffffffu);
-    const long long st = P.Q.size[t];
-    const long long si = V.msz[i];
-    const int qi = V.mq[i];
-    for (long long q = p - 1; q >= 0 && P.skey_sorted[q] == key; --q) {
-      const unsigned long long vj = P.sval_sorted[q];
-      const int j = static_cast<int>(vj >> 32);
-      const long long cj = static_cast<long long>(vj & 0xffffffffu);
-      const long long sj = V.msz[j];
-      const int qj = V.mq[j];
-      ++examined;
-      const long long oldc = EncodeCostForPair(qi, si, t, st, c) + EncodeCostForPair(qj, sj, t, st, cj);
-      const long long newc = EncodeCostForPair(qi, si + sj, t, st, c + cj);
-      const long long delta = oldc - newc;
-      if (delta > 0) {
-        atomicAdd(reinterpret_cast<unsigned long long*>(&pmat[static_cast<long long>(i) * g + j]),
-                  static_cast<unsigned long long>(delta));
-        atomicAdd(reinterpret_cast<unsigned long long*>(&pmat[static_cast<long long>(j) * g + i]),
-                  static_cast<unsigned long long>(delta));
+  const long long nchunks = (P.nslots + 31) >> 5;
+  const long long wstride = static_cast<long long>(gridDim.x) * (kAccumThreads / 32);
+  for (long long ch = (static_cast<long long>(blockIdx.x) * kAccumThreads + threadIdx.x) >> 5; ch < nchunks;
+       ch += wstride) {
+    const long long p0 = ch << 5;
+    const long long p = p0 + lane;
+    RunEntry me;
+    me.key = p < P.nslots ? P.skey_sorted[p] : kSlotPad;
+    me.c = me.s = 0;
+    me.i = me.q = 0;
+    const bool valid = me.key != kSlotPad && static_cast<int>(me.key >> 32) < P.nlist;
+    int t = 0, g = 0;
+    long long st = 0;
+    long long* pmat = nullptr;
+    if (valid) {
+      const int bl = static_cast<int>(me.key >> 32);
+      t = static_cast<int>(me.key & 0xffffffffu);
+      const int ri = P.list[P.list0 + bl];
+      g = P.glen[P.real[ri]];
+      pmat = reinterpret_cast<long long*>(P.mat + P.mat_off[ri]);
+      const RunEntry r = LoadRunEntry(P, p, Deferred(P.desc[P.list0 + bl].base, g));
+      me.c = r.c;
+      me.s = r.s;
+      me.i = r.i;
+      me.q = r.q;
+      st = P.Q.size[t];
+    }
+    // pairs inside the chunk
+    for (int src = 0; src < 31; ++src) {
+      const RunEntry o = ShflRunEntry(me, src);
+      if (valid && src < lane && o.key == me.key) AccumPair(me, o, t, st, g, pmat, examined);
+    }
+    // the run holding the chunk's first slot may start in earlier chunks
+    const unsigned long long first = __shfl_sync(0xffffffffu, me.key, 0);
+    if (first == kSlotPad || p0 == 0 || P.skey_sorted[p0 - 1] != first) continue;
+    const int fbl = static_cast<int>(first >> 32);
+    if (fbl >= P.nlist) continue;
+    const int fg = P.glen[P.real[P.list[P.list0 + fbl]]];
+    const DeferredView FV = Deferred(P.desc[P.list0 + fbl].base, fg);
+    const bool mine = valid && me.key == first;
+    for (long long c0 = p0 - 32;; c0 -= 32) {
+      // c0 >= 0: p0 is a multiple of 32 and slot p0 - 1 is in the run
+      RunEntry o;
+      o.key = P.skey_sorted[c0 + lane];
+      o.c = o.s = 0;
+      o.i = o.q = 0;
+      if (o.key == first) o = [&] { RunEntry r = LoadRunEntry(P, c0 + lane, FV); r.key = first; return r; }();
+      for (int src = 0; src < 32; ++src) {
+        const RunEntry b = ShflRunEntry(o, src);
+        if (mine && b.key == first) AccumPair(me, b, t, st, g, pmat, examined);
       }
+      if (c0 == 0 || __shfl_sync(0xffffffffu, o.key, 0) != first) break;
     }
   }
   examined = static_cast<unsigned long long>(WarpSum(static_cast<long long>(examined)));
-  if ((threadIdx.x & 31) == 0 && examined) atomicAdd(&P.stats[kStProxyExamined], examined);
+  if (lane == 0 && examined) atomicAdd(&P.stats[kStProxyExamined], examined);
 }
 
 // Member pass of the big groups: one warp per member of every group in the
@@ -2396,7 +2466,7 @@ __device__ __forceinline__ PlanSums PlanOfGroup(int g, unsigned e, long long k) 
   } else {
     f.big = 1;
     f.moff = gl;
-    f.soff = e > static_cast<unsigned>(kSmemEntries) ? static_cast<long long>(e) : 0;
+    f.soff = e > static_cast<unsigned>(kSmemEntries) || g > kSmemMaxGroup ? static_cast<long long>(e) : 0;
     f.mat = (OldCostOffset(gl * gl) + 8 * gl + 255) & ~255ll;
   }
   if (g <= kSelectSmallGroup) {
@@ -2571,6 +2641,7 @@ void Engine::PrepareIterationBuffers() {
   h_soff_.assign(1, 0);
   h_block_small_.clear();
   h_block_big_.clear();
+  std::vector<long long> block_mat;
   auto is_small = [&](int ri) {
     const size_t gid = static_cast<size_t>(h_real_[static_cast<size_t>(ri)]);
     return h_glen_[gid] <= kSmallGroup && h_gent_[gid] <= static_cast<unsigned>(kSmallStage);
@@ -2598,11 +2669,12 @@ void Engine::PrepareIterationBuffers() {
       h_big_moff_.push_back(h_big_moff_.back() + g);
       // groups beyond the shared-memory bucket table get sort slots
       const long long e_ub = h_gent_[gid];
-      h_soff_.push_back(h_soff_.back() + (e_ub > kSmemEntries ? e_ub : 0));
+      h_soff_.push_back(h_soff_.back() + (e_ub > kSmemEntries || g > kSmemMaxGroup ? e_ub : 0));
       h_mat_off_[static_cast<size_t>(ri)] = off;
       off += (OldCostOffset(g * g) + 8 * g + 255) & ~255ll;  // pair tables + old costs
     }
     max_mat = std::max(max_mat, off);
+    block_mat.push_back(off);
   }
   h_block_small_.push_back(static_cast<int>(h_small_.size()));
   h_block_big_.push_back(static_cast<int>(h_big_.size()));
@@ -2695,6 +2767,7 @@ void Engine::PrepareIterationBuffers() {
     for (int i = bp.b0; i < bp.b1; ++i) {
       bp.max_e = std::max(bp.max_e, h_soff_[static_cast<size_t>(i) + 1] - h_soff_[static_cast<size_t>(i)]);
     }
+    bp.mat_bytes = block_mat[b];
     bp.ss0 = h_block_sel_small_[b];
     bp.ss1 = h_block_sel_small_[b + 1];
     bp.sm0 = h_block_sel_mid_[b];
@@ -2804,6 +2877,7 @@ void Engine::PlanOnDevice() {
   bp.members = v[kPlanMembers];
   bp.nslots = v[kPlanSlots];
   bp.max_e = v[kPlanMaxE];
+  bp.mat_bytes = v[kPlanMat];
   bp.ss1 = static_cast<int>(v[kPlanSelSmall]);
   bp.sm1 = static_cast<int>(v[kPlanSelMid]);
   bp.sb1 = static_cast<int>(v[kPlanSelBig]);
@@ -2892,6 +2966,7 @@ void Engine::LaunchPrepare(const BlockPlan& bp) {
   PP.cand_cnt = d_cand_cnt_.p;
   PP.mat_off = d_mat_off_.p;
   PP.mat = d_mat_.p;
+  PP.mat_zeroed = 0;
   PP.scratch = d_scratch_.p;
   PP.scratch_cap = d_scratch_.n;
   PP.ctl = d_ctl_.p;
@@ -2919,6 +2994,12 @@ void Engine::LaunchPrepare(const BlockPlan& bp) {
     PP.soff = d_soff_.p;
     PP.slot0 = bp.slot0;
     PP.nslots = bp.nslots;
+    if (bp.rg1 - bp.rg0 > kFewGroups && bp.mat_bytes > 0) {
+      // one memset clears every pair table of a large block (a CTA clearing
+      // its own group's tables is the tail of the kernel for large groups)
+      CheckCuda(cudaMemsetAsync(d_mat_.p, 0, static_cast<size_t>(bp.mat_bytes), stream_), "memset pair tables");
+      PP.mat_zeroed = 1;
+    }
     PP.skey = d_skey_[0].p;
     PP.sval = d_sval_[0].p;
     PP.skey_sorted = d_skey_[1].p;
@@ -2940,7 +3021,7 @@ void Engine::LaunchPrepare(const BlockPlan& bp) {
       d_cub_tmp_.ensure(bytes);
       CheckCuda(cub::DeviceRadixSort::SortPairs(d_cub_tmp_.p, bytes, d_skey_[0].p, d_skey_[1].p, d_sval_[0].p,
                                                 d_sval_[1].p, PP.nslots, 0, bits, stream_), "cub radix sort");
-      const long long want = (PP.nslots + kAccumThreads - 1) / kAccumThreads;
+      const long long want = ((PP.nslots + 31) / 32 + kAccumThreads / 32 - 1) / (kAccumThreads / 32);
       ++launches_;
       PrepareAccumKernel<<<static_cast<int>(std::min(want, 152ll * 16)), kAccumThreads, 0, stream_>>>(PP);
     }
