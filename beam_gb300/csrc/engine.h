@@ -233,6 +233,7 @@ class Engine {
   void RankerTrain();
   void RankerFinishIteration();
   void LaunchPrepare(const BlockPlan& bp);
+  bool RowSumsOn(const BlockPlan& bp) const;
   void PlanOnDevice();
   void SizeIterationBuffers(size_t R, size_t ncand, size_t nsel, size_t nbig, long long max_mat, long long max_slots);
   void PrepareIterationBuffers();
@@ -316,6 +317,11 @@ class Engine {
   DevBuf<int> d_real_;
   std::vector<long long> h_cand_off_, h_sel_off_, h_mat_off_;
   std::vector<BlockPlan> plans_;  // this iteration's blocks
+  // per-row sums of a one-block iteration's block-start state (exact gain
+  // from the shared neighbours only)
+  DevBuf<long long> d_rc_before_, d_rc_light_;
+  DevBuf<int4> d_rc_heavy_;
+  DevBuf<int> d_rc_nheavy_;
   bool plan_on_device_ = false;   // one-block iteration: Merge plans it on the device
   DevBuf<unsigned char> d_plan_tiles_;
   DevBuf<long long> d_plan_scalars_;

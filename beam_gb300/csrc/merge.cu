@@ -67,6 +67,7 @@ __device__ __forceinline__ unsigned long long* ScratchAlloc(unsigned char* base,
 
 struct GainWork {
   long long raw_a, raw_b, uni, ovl;
+  long long bytes;  // algorithmic bytes of the gain computations
 };
 
 // Warp-cooperative ExactMergeGainPersistentImpl as a tiled merge of the two
@@ -169,6 +170,150 @@ __device__ void WarpExactGain(const QuotientView& Q, int a, int b, long long* ga
     work->raw_b += lb;
     work->uni += uni;
     work->ovl += ovl;
+    // 8 B per row entry, 4 B per union-neighbour size gather
+    work->bytes += 8ll * (la + lb) + 4ll * uni;
+  }
+}
+
+// Per-row sums of the block-start state, for WarpExactGainShared:
+//   before[r] = sum over the row of BlockCost(size_r, size_x, c_rx),
+//   light[r]  = sum of c_rx over the row's light entries,
+// where an entry is light when 1 + (size_r + 1) * size_x >= 2 c_rx: its
+// after-merge term min(c, 1 + s * size_x - c) is c for every merged size
+// s >= size_r + 1. The positions of the heavy entries are kept when there
+// are at most kHeavyMax of them; a row with more is scored by the full merge.
+constexpr int kHeavyMax = 4;
+
+struct RowConsts {
+  const long long* before;
+  const long long* light;
+  const int4* heavy;   // positions of the heavy entries, -1 unused
+  const int* nheavy;   // heavy entries of the row
+};
+
+// Row sums are written by the prepare kernels, which read every member row
+// of the block's groups with the target sizes anyway.
+__device__ __forceinline__ bool HeavyEntry(long long size_r, long long size_x, long long c) {
+  return 1 + (size_r + 1) * size_x < 2 * c;
+}
+
+// Warp-uniform call per 32-entry step of a row: records the positions of the
+// step's heavy entries after the nh found so far.
+__device__ __forceinline__ void RecordHeavy(int4* slot, int& nh, bool heavy, int k) {
+  const int lane = threadIdx.x & 31;
+  const unsigned hm = __ballot_sync(0xffffffffu, heavy);
+  if (heavy) {
+    const int rank = nh + __popc(hm & ((1u << lane) - 1u));
+    if (rank < kHeavyMax) reinterpret_cast<int*>(slot)[rank] = k;
+  }
+  nh += __popc(hm);
+}
+
+// ExactMergeGainPersistentImpl from the row sums: with s = size_a + size_b,
+//   before = before[a] + before[b] - BC(s_b, s_a, e_ab) + BC_int(a) + BC_int(b)
+//   after  = F_a(s) + F_b(s) - BC(s, s_b, e_ab) - BC(s, s_a, e_ab)
+//            + sum over shared x of [BC(s, s_x, c_ax + c_bx) - BC(s, s_x, c_ax) - BC(s, s_x, c_bx)]
+//            + BC_int(s, i_a + i_b + e_ab),
+// F_r(s) = light[r] + the heavy entries' exact terms. Only the shared
+// neighbours need sizes and cost terms; the tiled merge that finds them is
+// the one of WarpExactGain. The same integers as the full merge, term by
+// term regrouped.
+__device__ void WarpExactGainShared(const QuotientView& Q, const RowConsts& RC, int a, int b, long long* gain_out,
+                                    long long* before_out, GainWork* work, DevError* err) {
+  constexpr unsigned kFull = 0xffffffffu;
+  constexpr Entry kPadEntry = static_cast<Entry>(0x7fffffffull) << 32;
+  const int ha = RC.nheavy[a];
+  const int hb = RC.nheavy[b];
+  if (ha > kHeavyMax || hb > kHeavyMax) {
+    WarpExactGain(Q, a, b, gain_out, before_out, work, err);
+    return;
+  }
+  const int lane = threadIdx.x & 31;
+  const long long sa = Q.size[a];
+  const long long sb = Q.size[b];
+  const long long sw = sa + sb;
+  const Entry* ra = Q.ent + Q.off[a];
+  const Entry* rb = Q.ent + Q.off[b];
+  const int la = Q.len[a];
+  const int lb = Q.len[b];
+  long long shared = 0, eab_a = 0, eab_b = 0;
+  int ovl = 0, bad = 0;
+  int pa = 0, pb = 0;
+  while (pa < la || pb < lb) {
+    const bool va = pa + lane < la;
+    const bool vb = pb + lane < lb;
+    const Entry ea_e = va ? ra[pa + lane] : kPadEntry;
+    const Entry eb_e = vb ? rb[pb + lane] : kPadEntry;
+    const int xa = EntNb(ea_e);
+    const int xb = EntNb(eb_e);
+    const int last_a = __shfl_sync(kFull, xa, 31);
+    const int last_b = __shfl_sync(kFull, xb, 31);
+    const int lim = last_a < last_b ? last_a : last_b;
+    int pos_b = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+      const int probe_b = __shfl_sync(kFull, xb, pos_b + step - 1);
+      if (probe_b < xa) pos_b += step;
+    }
+    const Entry cand_b = __shfl_sync(kFull, eb_e, pos_b);
+    const bool fin_a = va && xa <= lim;
+    const bool fin_b = vb && xb <= lim;
+    if (fin_a) {
+      if (xa == b) {
+        eab_a = EntCnt(ea_e);
+      } else if (EntNb(cand_b) == xa) {
+        const long long ca = EntCnt(ea_e);
+        const long long cb = EntCnt(cand_b);
+        const long long sx = Q.size[xa];
+        shared += BlockCost(sw, sx, ca + cb, false, bad) - BlockCost(sw, sx, ca, false, bad) -
+                  BlockCost(sw, sx, cb, false, bad);
+        ++ovl;
+      }
+    }
+    if (fin_b && xb == a) eab_b = EntCnt(eb_e);
+    pa += __popc(__ballot_sync(kFull, fin_a));
+    pb += __popc(__ballot_sync(kFull, fin_b));
+  }
+  // heavy entries: lanes 0..3 of row a, lanes 4..7 of row b
+  long long heavy_a = 0, heavy_b = 0;
+  if (lane < 2 * kHeavyMax) {
+    const bool on_a = lane < kHeavyMax;
+    const int h = on_a ? lane : lane - kHeavyMax;
+    if (h < (on_a ? ha : hb)) {
+      const int4 hp = on_a ? RC.heavy[a] : RC.heavy[b];
+      const int pos = h == 0 ? hp.x : h == 1 ? hp.y : h == 2 ? hp.z : hp.w;
+      const Entry e = (on_a ? ra : rb)[pos];
+      const long long term = BlockCost(sw, Q.size[EntNb(e)], EntCnt(e), false, bad);
+      (on_a ? heavy_a : heavy_b) = term;
+    }
+  }
+  shared = WarpSum(shared);
+  heavy_a = WarpSum(heavy_a);
+  heavy_b = WarpSum(heavy_b);
+  eab_a = WarpMax(eab_a);
+  eab_b = WarpMax(eab_b);
+  ovl = WarpSumInt(ovl);
+  bad = __any_sync(kFull, bad);
+  if (eab_a != eab_b) {
+    if (lane == 0) RaiseError(err, kErrAsymmetric, a, b, 0);
+  }
+  const long long ia = Q.internal[a];
+  const long long ib = Q.internal[b];
+  const long long before = RC.before[a] + RC.before[b] - BlockCost(sb, sa, eab_b, false, bad) +
+                           BlockCost(sa, sa, ia, true, bad) + BlockCost(sb, sb, ib, true, bad);
+  const long long after = RC.light[a] + heavy_a + RC.light[b] + heavy_b - BlockCost(sw, sb, eab_a, false, bad) -
+                          BlockCost(sw, sa, eab_b, false, bad) + shared +
+                          BlockCost(sw, sw, ia + ib + eab_a, true, bad);
+  if (bad && lane == 0) RaiseError(err, kErrBlockCost, a, b, 0);
+  *gain_out = before - after;
+  *before_out = before;
+  if (work) {
+    work->raw_a += la;
+    work->raw_b += lb;
+    work->uni += (la - (eab_a > 0 ? 1 : 0)) + (lb - (eab_b > 0 ? 1 : 0)) - ovl;
+    work->ovl += ovl;
+    // 8 B per row entry, 4 B per shared-neighbour size gather, 36 B of row sums
+    work->bytes += 8ll * (la + lb) + 4ll * ovl + 36;
   }
 }
 
@@ -241,6 +386,11 @@ struct PrepareParams {
   const long long* mat_off;
   unsigned char* mat;
   int mat_zeroed;  // the pair tables were cleared by one memset of the block
+  // row sums for the scoring pass (rc_before == nullptr: not needed)
+  long long* rc_before;
+  long long* rc_light;
+  int4* rc_heavy;
+  int* rc_nheavy;
   unsigned char* scratch;
   unsigned long long scratch_cap;
   BlockCtl* ctl;
@@ -387,6 +537,13 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
       const long long si = S.sz[i];
       const long long internal = Q.internal[S.q[i]];
       old_out[i] = internal > 0 ? EncodeCostForPair(S.q[i], si, S.q[i], si, 2 * internal) : 0;
+      if (P.rc_before) {
+        // the fill pass adds the row sums
+        P.rc_before[S.q[i]] = 0;
+        P.rc_light[S.q[i]] = 0;
+        P.rc_nheavy[S.q[i]] = 0;
+        P.rc_heavy[S.q[i]] = make_int4(-1, -1, -1, -1);
+      }
     }
     if (tid == 0) V.eoff[g] = E;
     if (!P.mat_zeroed) {
@@ -435,23 +592,39 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
     const Entry* row = Q.ent + S.off[i];
     const int len = S.len[i];
     const int eo = S.eoff[i];
-    long long old = 0;
-    for (int k = lane; k < len; k += 32) {
-      const Entry e = row[k];
-      const int t = EntNb(e);
-      const long long c = EntCnt(e);
-      const long long st = Q.size[t];
-      old += EncodeCostForPair(rep, si, t, st, c);
-      et[eo + k] = t;
-      ei[eo + k] = i;
-      ee[eo + k] = static_cast<unsigned>(c);
-      enx[eo + k] = atomicExch(&heads[BucketHash(t, hmask)], eo + k);
-      // direct in-group edge: row i holds j and row j holds i with the same
-      // count, so each half of the table gets it once
-      if (P.group_of[t] == gid) pmat[static_cast<long long>(i) * g + P.idx_in_group[t]] = c;
+    long long old = 0, light = 0;
+    int nh = 0;
+    if (P.rc_before && lane == 0) P.rc_heavy[rep] = make_int4(-1, -1, -1, -1);
+    __syncwarp();
+    for (int k0 = 0; k0 < len; k0 += 32) {
+      const int k = k0 + lane;
+      bool heavy = false;
+      if (k < len) {
+        const Entry e = row[k];
+        const int t = EntNb(e);
+        const long long c = EntCnt(e);
+        const long long st = Q.size[t];
+        old += EncodeCostForPair(rep, si, t, st, c);
+        heavy = HeavyEntry(si, st, c);
+        if (!heavy) light += c;
+        et[eo + k] = t;
+        ei[eo + k] = i;
+        ee[eo + k] = static_cast<unsigned>(c);
+        enx[eo + k] = atomicExch(&heads[BucketHash(t, hmask)], eo + k);
+        // direct in-group edge: row i holds j and row j holds i with the same
+        // count, so each half of the table gets it once
+        if (P.group_of[t] == gid) pmat[static_cast<long long>(i) * g + P.idx_in_group[t]] = c;
+      }
+      if (P.rc_before) RecordHeavy(P.rc_heavy + rep, nh, heavy, k);
     }
     old = WarpSum(old);
+    if (P.rc_before) light = WarpSum(light);
     if (lane == 0) {
+      if (P.rc_before) {
+        P.rc_before[rep] = old;
+        P.rc_light[rep] = light;
+        P.rc_nheavy[rep] = nh;
+      }
       const long long internal = Q.internal[rep];
       if (internal > 0) old += EncodeCostForPair(rep, si, rep, si, 2 * internal);
       S.old[i] = old;
@@ -540,7 +713,7 @@ __global__ void __launch_bounds__(kFillThreads) PrepareFillKernel(PrepareParams 
   for (int base = blockIdx.y * kFillThreads; base < d.E; base += stride) {
     const int idx = base + threadIdx.x;
     int i = -1;
-    long long cost = 0;
+    long long cost = 0, light = 0;
     if (idx < d.E) {
       int lo = 0, hi = g;  // last member with eoff <= idx
       while (hi - lo > 1) {
@@ -552,7 +725,16 @@ __global__ void __launch_bounds__(kFillThreads) PrepareFillKernel(PrepareParams 
       const Entry e = Q.ent[Q.off[rep] + (idx - eoff_s[i])];
       const int t = EntNb(e);
       const long long c = EntCnt(e);
-      cost = EncodeCostForPair(rep, V.msz[i], t, Q.size[t], c);
+      const long long st = Q.size[t];
+      cost = EncodeCostForPair(rep, V.msz[i], t, st, c);
+      if (P.rc_before) {
+        if (HeavyEntry(V.msz[i], st, c)) {
+          const int rank = atomicAdd(&P.rc_nheavy[rep], 1);
+          if (rank < kHeavyMax) reinterpret_cast<int*>(&P.rc_heavy[rep])[rank] = idx - eoff_s[i];
+        } else {
+          light = c;
+        }
+      }
       P.skey[slot + idx] = key_hi | static_cast<unsigned>(t);
       P.sval[slot + idx] = static_cast<unsigned long long>(i) << 32 | static_cast<unsigned long long>(c);
       if (P.group_of[t] == gid) pmat[static_cast<long long>(i) * g + P.idx_in_group[t]] = c;
@@ -560,12 +742,21 @@ __global__ void __launch_bounds__(kFillThreads) PrepareFillKernel(PrepareParams 
     // segmented inclusive scan over runs of equal member index
     for (int o = 1; o < 32; o <<= 1) {
       const long long vc = __shfl_up_sync(0xffffffffu, cost, o);
+      const long long vl = __shfl_up_sync(0xffffffffu, light, o);
       const int vi = __shfl_up_sync(0xffffffffu, i, o);
-      if (lane >= o && vi == i) cost += vc;
+      if (lane >= o && vi == i) {
+        cost += vc;
+        light += vl;
+      }
     }
     const int next_i = __shfl_down_sync(0xffffffffu, i, 1);
-    if (i >= 0 && (lane == 31 || next_i != i) && cost != 0) {
-      atomicAdd(&old_out[i], static_cast<unsigned long long>(cost));
+    if (i >= 0 && (lane == 31 || next_i != i)) {
+      if (cost != 0) atomicAdd(&old_out[i], static_cast<unsigned long long>(cost));
+      if (P.rc_before) {
+        const int rep = V.mq[i];
+        if (cost != 0) atomicAdd(reinterpret_cast<unsigned long long*>(&P.rc_before[rep]), static_cast<unsigned long long>(cost));
+        if (light != 0) atomicAdd(reinterpret_cast<unsigned long long*>(&P.rc_light[rep]), static_cast<unsigned long long>(light));
+      }
     }
   }
 }
@@ -1083,9 +1274,26 @@ __global__ void __launch_bounds__(kSmallWarps * 32) PrepareSmallKernel(PreparePa
     if (lane < g) {
       const int rep = S.q[lane];
       const long long si = S.sz[lane];
-      long long old = 0;
+      long long old = 0, light = 0;
+      int nh = 0;
+      int4 hp = make_int4(-1, -1, -1, -1);
       for (int k = S.start[lane]; k < S.start[lane + 1]; ++k) {
-        old += EncodeCostForPair(rep, si, EntNb(S.ent[k]), S.tsz[k], EntCnt(S.ent[k]));
+        const long long c = EntCnt(S.ent[k]);
+        const long long st = S.tsz[k];
+        old += EncodeCostForPair(rep, si, EntNb(S.ent[k]), st, c);
+        if (HeavyEntry(si, st, c)) {
+          const int pos = k - S.start[lane];
+          if (nh == 0) hp.x = pos; else if (nh == 1) hp.y = pos; else if (nh == 2) hp.z = pos; else if (nh == 3) hp.w = pos;
+          ++nh;
+        } else {
+          light += c;
+        }
+      }
+      if (P.rc_before) {
+        P.rc_before[rep] = old;
+        P.rc_light[rep] = light;
+        P.rc_heavy[rep] = hp;
+        P.rc_nheavy[rep] = nh;
       }
       const long long internal = Q.internal[rep];
       if (internal > 0) old += EncodeCostForPair(rep, si, rep, si, 2 * internal);
@@ -1138,13 +1346,31 @@ __global__ void __launch_bounds__(kSmallWarps * 32) PrepareSmallKernel(PreparePa
       const long long si = S.sz[i];
       const long long oi = __shfl_sync(0xffffffffu, off, i);
       const int li2 = S.len[i];
-      long long old = 0;
-      for (int k = lane; k < li2; k += 32) {
-        const Entry e = Q.ent[oi + k];
-        old += EncodeCostForPair(rep, si, EntNb(e), Q.size[EntNb(e)], EntCnt(e));
+      long long old = 0, light = 0;
+      int nh = 0;
+      if (P.rc_before && lane == 0) P.rc_heavy[rep] = make_int4(-1, -1, -1, -1);
+      __syncwarp();
+      for (int k0 = 0; k0 < li2; k0 += 32) {
+        const int k = k0 + lane;
+        bool heavy = false;
+        if (k < li2) {
+          const Entry e = Q.ent[oi + k];
+          const long long c = EntCnt(e);
+          const long long st = Q.size[EntNb(e)];
+          old += EncodeCostForPair(rep, si, EntNb(e), st, c);
+          heavy = HeavyEntry(si, st, c);
+          if (!heavy) light += c;
+        }
+        if (P.rc_before) RecordHeavy(P.rc_heavy + rep, nh, heavy, k);
       }
       old = WarpSum(old);
+      if (P.rc_before) light = WarpSum(light);
       if (lane == 0) {
+        if (P.rc_before) {
+          P.rc_before[rep] = old;
+          P.rc_light[rep] = light;
+          P.rc_nheavy[rep] = nh;
+        }
         const long long internal = Q.internal[rep];
         if (internal > 0) old += EncodeCostForPair(rep, si, rep, si, 2 * internal);
         S.old[i] = old;
@@ -1296,9 +1522,19 @@ struct ScoreParams {
   int audit;          // phase 2: score pruned slots aside and count the ones the filter passes
   double threshold;
   int use_threshold;
+  RowConsts rc;  // row sums of the block-start state (rc.before == nullptr: full merge)
   unsigned long long* stats;
   DevError* err;
 };
+
+__device__ __forceinline__ void ScoreGain(const ScoreParams& P, int a, int b, long long* gain, long long* before,
+                                          GainWork* w) {
+  if (P.rc.before) {
+    WarpExactGainShared(P.Q, P.rc, a, b, gain, before, w, P.err);
+  } else {
+    WarpExactGain(P.Q, a, b, gain, before, w, P.err);
+  }
+}
 
 __device__ __forceinline__ bool PassesFilter(long long gain, long long before, double threshold, int use_threshold) {
   if (gain <= 0) return false;
@@ -1315,10 +1551,8 @@ __device__ __forceinline__ void FlushScoreStats(unsigned long long* stats, const
   atomicAdd(&stats[kStRawB], static_cast<unsigned long long>(w.raw_b));
   atomicAdd(&stats[kStUnion], static_cast<unsigned long long>(w.uni));
   atomicAdd(&stats[kStOverlap], static_cast<unsigned long long>(w.ovl));
-  // algorithmic bytes: 8 B per row entry read, 4 B per union-neighbour size
-  // gather, 8 B pair + 16 B result per pair
-  atomicAdd(&stats[kStScoreBytes],
-            static_cast<unsigned long long>(8 * (w.raw_a + w.raw_b) + 4 * w.uni + 24 * pairs));
+  // algorithmic bytes: the gain computations' own, 8 B pair + 16 B result per pair
+  atomicAdd(&stats[kStScoreBytes], static_cast<unsigned long long>(w.bytes + 24 * pairs));
 }
 
 // One warp per candidate slot of the block (the concatenated per-group
@@ -1330,7 +1564,7 @@ __global__ void __launch_bounds__(kScoreThreads) ScoreKernel(ScoreParams P) {
   const int lane = threadIdx.x & 31;
   const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const long long nw = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
-  GainWork w = {0, 0, 0, 0};
+  GainWork w = {0, 0, 0, 0, 0};
   long long pairs = 0, view_nnz = 0;
   unsigned long long pruned = 0;
   const float cutoff = P.phase == 2 ? *P.cutoff : 0.0f;
@@ -1346,8 +1580,8 @@ __global__ void __launch_bounds__(kScoreThreads) ScoreKernel(ScoreParams P) {
       if (P.zbuf[slot] < cutoff) {
         // pruned by the ranker: not scored (the audit scores it aside)
         if (P.audit) {
-          GainWork aw = {0, 0, 0, 0};
-          WarpExactGain(P.Q, a, b, &gain, &before, &aw, P.err);
+          GainWork aw = {0, 0, 0, 0, 0};
+          ScoreGain(P, a, b, &gain, &before, &aw);
           if (lane == 0 && PassesFilter(gain, before, P.threshold, P.use_threshold)) {
             atomicAdd(&P.stats[kStRkAuditPassing], 1ull);
             atomicAdd(&P.stats[kStRkAuditLost], 1ull);
@@ -1360,7 +1594,7 @@ __global__ void __launch_bounds__(kScoreThreads) ScoreKernel(ScoreParams P) {
         continue;
       }
     }
-    WarpExactGain(P.Q, a, b, &gain, &before, &w, P.err);
+    ScoreGain(P, a, b, &gain, &before, &w);
     if (lane == 0) {
       if (P.phase != 0 && PassesFilter(gain, before, P.threshold, P.use_threshold)) {
         if (P.audit) atomicAdd(&P.stats[kStRkAuditPassing], 1ull);
@@ -2951,6 +3185,11 @@ void Engine::LaunchCommit(int rg0, int nrg, int64_t max_pairs, bool verify) {
 
 // EA-proxy candidates for the small-group list entries [s0, s1) (one warp
 // per group) and the big-group entries [b0, b1) (one CTA per group).
+// Row sums for the scoring pass: in a large block of a one-block iteration
+// (the prepare kernels write them while reading the member rows; scoring from
+// them pays in a large block).
+bool Engine::RowSumsOn(const BlockPlan& bp) const { return plans_.size() == 1 && bp.rg1 - bp.rg0 > kFewGroups; }
+
 void Engine::LaunchPrepare(const BlockPlan& bp) {
   const int s0 = bp.s0, s1 = bp.s1, b0 = bp.b0, b1 = bp.b1;
   PrepareParams PP;
@@ -2967,6 +3206,20 @@ void Engine::LaunchPrepare(const BlockPlan& bp) {
   PP.mat_off = d_mat_off_.p;
   PP.mat = d_mat_.p;
   PP.mat_zeroed = 0;
+  PP.rc_before = nullptr;
+  PP.rc_light = nullptr;
+  PP.rc_heavy = nullptr;
+  PP.rc_nheavy = nullptr;
+  if (RowSumsOn(bp)) {
+    d_rc_before_.ensure(static_cast<size_t>(n_));
+    d_rc_light_.ensure(static_cast<size_t>(n_));
+    d_rc_heavy_.ensure(static_cast<size_t>(n_));
+    d_rc_nheavy_.ensure(static_cast<size_t>(n_));
+    PP.rc_before = d_rc_before_.p;
+    PP.rc_light = d_rc_light_.p;
+    PP.rc_heavy = d_rc_heavy_.p;
+    PP.rc_nheavy = d_rc_nheavy_.p;
+  }
   PP.scratch = d_scratch_.p;
   PP.scratch_cap = d_scratch_.n;
   PP.ctl = d_ctl_.p;
@@ -3067,6 +3320,11 @@ void Engine::RunBlock(const BlockPlan& bp, double threshold, int iter, int total
   SP.npos = d_rk_npos_.p;
   SP.zcap = 0;
   SP.cutoff = d_rk_cut_.p;
+  SP.rc = RowConsts{nullptr, nullptr, nullptr, nullptr};
+  if (RowSumsOn(bp)) {
+    // written by this block's prepare kernels
+    SP.rc = RowConsts{d_rc_before_.p, d_rc_light_.p, d_rc_heavy_.p, d_rc_nheavy_.p};
+  }
   const int sgrid = static_cast<int>(std::min<long long>((slots + 7) / 8, 152 * 16));
   // learned ranker: trained after the logging iterations; afterwards the
   // exploration subset is scored first, then the rest above the cutoff
