@@ -209,6 +209,21 @@ __device__ __forceinline__ void RecordHeavy(int4* slot, int& nh, bool heavy, int
   nh += __popc(hm);
 }
 
+// Skewed pairs (the long row at least kProbeMinLong entries and kProbeRatio
+// times the short one) look the short row up in the long one.
+constexpr int kProbeMinLong = 256;
+constexpr int kProbeRatio = 8;
+
+// First position of a sorted row whose neighbour is >= x.
+__device__ __forceinline__ int RowLowerBound(const Entry* row, int len, int x) {
+  int lo = 0, hi = len;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (EntNb(row[mid]) < x) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
 // ExactMergeGainPersistentImpl from the row sums: with s = size_a + size_b,
 //   before = before[a] + before[b] - BC(s_b, s_a, e_ab) + BC_int(a) + BC_int(b)
 //   after  = F_a(s) + F_b(s) - BC(s, s_b, e_ab) - BC(s, s_a, e_ab)
@@ -238,7 +253,50 @@ __device__ void WarpExactGainShared(const QuotientView& Q, const RowConsts& RC, 
   const int lb = Q.len[b];
   long long shared = 0, eab_a = 0, eab_b = 0;
   int ovl = 0, bad = 0;
-  int pa = 0, pb = 0;
+  const bool a_long = la >= lb;
+  const int ll = a_long ? la : lb;
+  const int ls = a_long ? lb : la;
+  const bool probe = ll >= kProbeMinLong && ll >= kProbeRatio * ls;
+  if (probe) {
+    // skewed pair: each entry of the short row is looked up in the long row
+    // by binary search instead of streaming the long row
+    const Entry* rl = a_long ? ra : rb;
+    const Entry* rs = a_long ? rb : ra;
+    const int long_rep = a_long ? a : b;
+    const int short_rep = a_long ? b : a;
+    long long e_long = 0, e_short = 0;  // e(a, b) as read from the long / the short row
+    for (int k0 = 0; k0 < ls; k0 += 32) {
+      const int k = k0 + lane;
+      if (k < ls) {
+        const Entry e = rs[k];
+        const int x = EntNb(e);
+        const long long cs = EntCnt(e);
+        if (x == long_rep) {
+          e_short = cs;
+        } else {
+          const int at = RowLowerBound(rl, ll, x);
+          if (at < ll && EntNb(rl[at]) == x) {
+            const long long cl = EntCnt(rl[at]);
+            const long long ca = a_long ? cl : cs;
+            const long long cb = a_long ? cs : cl;
+            const long long sx = Q.size[x];
+            shared += BlockCost(sw, sx, ca + cb, false, bad) - BlockCost(sw, sx, ca, false, bad) -
+                      BlockCost(sw, sx, cb, false, bad);
+            ++ovl;
+          }
+        }
+      }
+    }
+    if (lane == 0) {
+      const int at = RowLowerBound(rl, ll, short_rep);
+      if (at < ll && EntNb(rl[at]) == short_rep) e_long = EntCnt(rl[at]);
+    }
+    eab_a = a_long ? e_long : e_short;
+    eab_b = a_long ? e_short : e_long;
+  }
+  // otherwise the tiled merge of the two rows
+  int pa = probe ? la : 0;
+  int pb = probe ? lb : 0;
   while (pa < la || pb < lb) {
     const bool va = pa + lane < la;
     const bool vb = pb + lane < lb;
