@@ -1483,36 +1483,47 @@ __global__ void __launch_bounds__(kSmallWarps * 32) PrepareSmallKernel(PreparePa
     for (int j = i + 1; j < g; ++j) {
       if (S.p[TriIndex(i, j, g)] > 0) atomicOr(&S.fmask[i], 1u << j);
     }
-  } else if (lane < g) {
-    const int i = lane;
-    const int qi = S.q[i];
-    RankKey lst[kLaneTopK];
-    int nl = 0;
-    for (int j = 0; j < g; ++j) {
-      if (j == i) continue;
-      const long long pg = S.p[i < j ? TriIndex(i, j, g) : TriIndex(j, i, g)];
-      if (pg <= 0) continue;
-      long long denom = S.old[i] + S.old[j];
-      if (denom < 1) denom = 1;
-      RankKey k;
-      k.j = j;
-      k.pg = pg;
-      k.ratio = static_cast<double>(pg) / static_cast<double>(denom);
-      const int qj = S.q[j];
-      k.lo = qi < qj ? qi : qj;
-      k.hi = qi < qj ? qj : qi;
-      if (nl == top_k && !Better(k, lst[nl - 1])) continue;
-      int pos = nl < top_k ? nl : top_k - 1;
-      while (pos > 0 && Better(k, lst[pos - 1])) {
-        lst[pos] = lst[pos - 1];
-        --pos;
+  } else if (g - 1 > P.top_k) {
+    // ranking, one member at a time by the whole warp, lane j holding
+    // partner j: a partner's rank is the number of partners better than it
+    // under ranked_better (ratio desc, proxy gain desc, rep_lo asc, rep_hi
+    // asc), and the top_k ranks are kept. The ratio is the same correctly
+    // rounded double as the reference's; positive doubles order like their
+    // bit patterns, so every comparison is an integer one.
+    const int j = lane;
+    for (int i = 0; i < g; ++i) {
+      long long pg = 0;
+      if (j < g && j != i) pg = S.p[i < j ? TriIndex(i, j, g) : TriIndex(j, i, g)];
+      const bool valid = pg > 0;
+      const unsigned vm = __ballot_sync(0xffffffffu, valid);
+      const int cnt = __popc(vm);
+      if (cnt <= top_k) {
+        if (valid) atomicOr(&S.fmask[i < j ? i : j], 1u << (i < j ? j : i));
+        continue;
       }
-      lst[pos] = k;
-      if (nl < top_k) ++nl;
-    }
-    for (int r = 0; r < nl; ++r) {
-      const int j = lst[r].j;
-      atomicOr(&S.fmask[i < j ? i : j], 1u << (i < j ? j : i));
+      long long rbits = 0;
+      int lo = 0, hi = 0;
+      if (valid) {
+        long long denom = S.old[i] + S.old[j];
+        if (denom < 1) denom = 1;
+        rbits = __double_as_longlong(static_cast<double>(pg) / static_cast<double>(denom));
+        const int qi = S.q[i];
+        const int qj = S.q[j];
+        lo = qi < qj ? qi : qj;
+        hi = qi < qj ? qj : qi;
+      }
+      int rank = 0;
+      for (unsigned rest = vm; rest; rest &= rest - 1) {
+        const int o = __ffs(rest) - 1;
+        const long long orb = __shfl_sync(0xffffffffu, rbits, o);
+        const long long opg = __shfl_sync(0xffffffffu, pg, o);
+        const int olo = __shfl_sync(0xffffffffu, lo, o);
+        const int ohi = __shfl_sync(0xffffffffu, hi, o);
+        const bool better =
+            orb != rbits ? orb > rbits : opg != pg ? opg > pg : olo != lo ? olo < lo : ohi < hi;
+        rank += (valid && o != j && better) ? 1 : 0;
+      }
+      if (valid && rank < top_k) atomicOr(&S.fmask[i < j ? i : j], 1u << (i < j ? j : i));
     }
   }
   __syncwarp();
