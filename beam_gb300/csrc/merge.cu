@@ -1165,6 +1165,18 @@ __global__ void __launch_bounds__(256) PrepareMembersKernel(PrepareParams P) {
   }
 }
 
+// Flag bytes (0 or 1) of table word w that lie in [beg, end), as a bit set
+// with one bit per set flag (bit 8k for byte k).
+__device__ __forceinline__ unsigned long long RowFlagBits(const unsigned long long* fw, long long w, long long beg,
+                                                          long long end) {
+  const long long lo = beg - w * 8;  // first byte of the range in this word
+  const long long hi = end - w * 8;  // one past the last
+  unsigned long long m = 0x0101010101010101ull;
+  if (lo > 0) m &= ~0ull << (8 * lo);
+  if (hi < 8) m &= (1ull << (8 * hi)) - 1ull;
+  return fw[w] & m;
+}
+
 // Output pass of the big groups: the union of kept pairs in (a_idx, b_idx)
 // order, one CTA per group.
 __global__ void __launch_bounds__(kPrepThreads) PrepareOutputKernel(PrepareParams P) {
@@ -1184,14 +1196,17 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareOutputKernel(PrepareParam
   const long long* pmat = reinterpret_cast<const long long*>(P.mat + P.mat_off[ri]);
   const long long* old = reinterpret_cast<const long long*>(P.mat + P.mat_off[ri] + OldCostOffset(gg));
   const int* q = P.order + P.gstart[gid];
-  // union of kept pairs in (a_idx, b_idx) order
+  // union of kept pairs in (a_idx, b_idx) order. The flags of row a,
+  // bytes [a*g + a + 1, a*g + g) of the table, are read as 8-byte words
+  // (the table starts 8-byte aligned; the masked bytes past its end lie in
+  // the group's old-cost array).
+  const unsigned long long* fw = reinterpret_cast<const unsigned long long*>(fmat);
   for (int a = warp; a < g; a += nwarps) {
+    const long long beg = static_cast<long long>(a) * g + a + 1;
+    const long long end = static_cast<long long>(a) * g + g;
     int cnt = 0;
-    for (int base = a + 1; base < g; base += 32) {
-      const int b = base + lane;
-      const bool f = b < g && fmat[static_cast<long long>(a) * g + b];
-      cnt += __popc(__ballot_sync(0xffffffffu, f));
-    }
+    for (long long w = (beg >> 3) + lane; w < (end + 7) >> 3; w += 32) cnt += __popcll(RowFlagBits(fw, w, beg, end));
+    cnt = WarpSumInt(cnt);
     if (lane == 0) eoff[a] = cnt;
   }
   __syncthreads();
@@ -1211,13 +1226,24 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareOutputKernel(PrepareParam
   const int nc = carry;
   int2* out = P.cand + P.cand_off[ri];
   for (int a = warp; a < g; a += nwarps) {
+    const long long beg = static_cast<long long>(a) * g + a + 1;
+    const long long end = static_cast<long long>(a) * g + g;
+    const long long row0 = static_cast<long long>(a) * g;
     int pos = eoff[a];
-    for (int base = a + 1; base < g; base += 32) {
-      const int b = base + lane;
-      const bool f = b < g && fmat[static_cast<long long>(a) * g + b];
-      const unsigned ball = __ballot_sync(0xffffffffu, f);
-      if (f) {
-        const long long at = pos + __popc(ball & ((1u << lane) - 1u));
+    for (long long w0 = beg >> 3; w0 < (end + 7) >> 3; w0 += 32) {
+      const long long w = w0 + lane;
+      unsigned long long bits = w < (end + 7) >> 3 ? RowFlagBits(fw, w, beg, end) : 0ull;
+      const int c = __popcll(bits);
+      int incl = c;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      long long at = pos + incl - c;
+      while (bits) {
+        const int k = (__ffsll(static_cast<long long>(bits)) - 1) >> 3;
+        bits &= bits - 1;
+        const int b = static_cast<int>(w * 8 + k - row0);
         out[at] = make_int2(a, b);
         P.cand_rep[P.cand_off[ri] + at] = make_int2(q[a], q[b]);
         if (P.cand_feat) {
@@ -1227,8 +1253,9 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareOutputKernel(PrepareParam
           P.cand_feat[P.cand_off[ri] + at] =
               make_float2(static_cast<float>(pg), static_cast<float>(static_cast<double>(pg) / denom));
         }
+        ++at;
       }
-      pos += __popc(ball);
+      pos += __shfl_sync(0xffffffffu, incl, 31);
     }
   }
   if (tid == 0) {
