@@ -433,6 +433,7 @@ struct PrepareParams {
   int2* cand_rep;         // per candidate slot: the pair's supernode ids (unused slots stay -1)
   const long long* soff;  // sort-slot prefix over the big-group list (0 slots: not deferred)
   long long slot0;        // soff of the launch's first entry
+  int tbits;                 // bits of a target supernode id in a sort key
   unsigned long long* skey;  // unsorted keys / values of the launch's slots
   unsigned long long* sval;
   const unsigned long long* skey_sorted;
@@ -763,7 +764,7 @@ __global__ void __launch_bounds__(kFillThreads) PrepareFillKernel(PrepareParams 
   unsigned long long* old_out = reinterpret_cast<unsigned long long*>(mat + OldCostOffset(gg));
   const DeferredView V = Deferred(d.base, g);
   const long long slot = P.soff[P.list0 + blockIdx.x] - P.slot0;
-  const unsigned long long key_hi = static_cast<unsigned long long>(blockIdx.x) << 32;
+  const unsigned long long key_hi = static_cast<unsigned long long>(blockIdx.x) << P.tbits;
   for (int i = threadIdx.x; i <= g; i += kFillThreads) eoff_s[i] = V.eoff[i];
   __syncthreads();
   const QuotientView& Q = P.Q;
@@ -879,13 +880,13 @@ __global__ void __launch_bounds__(kAccumThreads) PrepareAccumKernel(PrepareParam
     me.key = p < P.nslots ? P.skey_sorted[p] : kSlotPad;
     me.c = me.s = 0;
     me.i = me.q = 0;
-    const bool valid = me.key != kSlotPad && static_cast<int>(me.key >> 32) < P.nlist;
+    const bool valid = me.key != kSlotPad && static_cast<int>(me.key >> P.tbits) < P.nlist;
     int t = 0, g = 0;
     long long st = 0;
     long long* pmat = nullptr;
     if (valid) {
-      const int bl = static_cast<int>(me.key >> 32);
-      t = static_cast<int>(me.key & 0xffffffffu);
+      const int bl = static_cast<int>(me.key >> P.tbits);
+      t = static_cast<int>(me.key & ((1ull << P.tbits) - 1ull));
       const int ri = P.list[P.list0 + bl];
       g = P.glen[P.real[ri]];
       pmat = reinterpret_cast<long long*>(P.mat + P.mat_off[ri]);
@@ -904,7 +905,7 @@ __global__ void __launch_bounds__(kAccumThreads) PrepareAccumKernel(PrepareParam
     // the run holding the chunk's first slot may start in earlier chunks
     const unsigned long long first = __shfl_sync(0xffffffffu, me.key, 0);
     if (first == kSlotPad || p0 == 0 || P.skey_sorted[p0 - 1] != first) continue;
-    const int fbl = static_cast<int>(first >> 32);
+    const int fbl = static_cast<int>(first >> P.tbits);
     if (fbl >= P.nlist) continue;
     const int fg = P.glen[P.real[P.list[P.list0 + fbl]]];
     const DeferredView FV = Deferred(P.desc[P.list0 + fbl].base, fg);
@@ -3349,6 +3350,8 @@ void Engine::LaunchPrepare(const BlockPlan& bp) {
       CheckCuda(cudaMemsetAsync(d_mat_.p, 0, static_cast<size_t>(bp.mat_bytes), stream_), "memset pair tables");
       PP.mat_zeroed = 1;
     }
+    PP.tbits = 1;
+    while ((1ll << PP.tbits) < n_) ++PP.tbits;
     PP.skey = d_skey_[0].p;
     PP.sval = d_sval_[0].p;
     PP.skey_sorted = d_skey_[1].p;
@@ -3362,8 +3365,10 @@ void Engine::LaunchPrepare(const BlockPlan& bp) {
       const unsigned slices = static_cast<unsigned>(std::min(512ll, std::max(1ll, (max_e + 2047) / 2048)));
       ++launches_;
       PrepareFillKernel<<<dim3(b1 - b0, slices), kFillThreads, 0, stream_>>>(PP);
-      int bits = 32;
-      while ((1ll << (bits - 32)) < b1 - b0) ++bits;
+      // key = launch-local group index << tbits | target; the group index
+      // stays below 2^(bits - tbits) - 1, so no key has the padding's low bits
+      int bits = PP.tbits;
+      while ((1ll << (bits - PP.tbits)) <= b1 - b0) ++bits;
       size_t bytes = 0;
       CheckCuda(cub::DeviceRadixSort::SortPairs(nullptr, bytes, d_skey_[0].p, d_skey_[1].p, d_sval_[0].p,
                                                 d_sval_[1].p, PP.nslots, 0, bits, stream_), "cub radix sort size");
