@@ -928,6 +928,157 @@ __global__ void __launch_bounds__(kAccumThreads) PrepareAccumKernel(PrepareParam
   if (lane == 0 && examined) atomicAdd(&P.stats[kStProxyExamined], examined);
 }
 
+// Top-k partners of member i of a big group whose partners fill NT slots of
+// 32 (the fp32 prescreen branch of PrepareMembersKernel).
+template <int NT>
+__device__ __forceinline__ void MembersTopK(int lane, int g, int i, int qi, int top_k, int cnt, const long long* prow,
+                                            const long long* old, long long old_i, const int* q, int* cj,
+                                            unsigned char* fmat) {
+  auto ratio_of = [&](int j, long long pg) {
+    long long denom = old_i + old[j];
+    if (denom < 1) denom = 1;
+    return static_cast<double>(pg) / static_cast<double>(denom);
+  };
+  // fp32 prescreen: the exact (double) ratio is only computed for the
+  // candidates that can be in the member's top_k. The fp32 ratio of a
+  // candidate is within relative 3 * 2^-24 of its double ratio, so every
+  // candidate of the exact top_k has an fp32 ratio >= tau * (1 - 2^-20),
+  // where tau is the top_k-th largest fp32 ratio (found by bisection on the
+  // float bit patterns, which order like the positive values).
+  float rf[NT];
+#pragma unroll
+  for (int t = 0; t < NT; ++t) {
+    const int j = lane + 32 * t;
+    float v = 0.0f;  // not a candidate
+    if (j < g && j != i) {
+      const long long pg = prow[j];
+      if (pg > 0) {
+        long long denom = old_i + old[j];
+        if (denom < 1) denom = 1;
+        v = __fdiv_rn(static_cast<float>(pg), static_cast<float>(denom));
+      }
+    }
+    rf[t] = v;
+  }
+  float cut = 0.0f;
+  if (cnt > top_k + 16) {
+    unsigned lo = 0, hi = 0x7f800000u;  // count(bits >= lo) >= top_k > count(bits >= hi)
+    while (hi - lo > 1) {
+      const unsigned mid = lo + ((hi - lo) >> 1);
+      int c = 0;
+#pragma unroll
+      for (int t = 0; t < NT; ++t) c += __float_as_uint(rf[t]) >= mid ? 1 : 0;
+      c = WarpSumInt(c);
+      if (c >= top_k) lo = mid; else hi = mid;
+    }
+    cut = __uint_as_float(lo) * (1.0f - 9.5367431640625e-7f);
+  }
+  int npass = 0;
+#pragma unroll
+  for (int t = 0; t < NT; ++t) npass += (rf[t] > 0.0f && rf[t] >= cut) ? 1 : 0;
+  npass = WarpSumInt(npass);
+  if (npass <= 32) {
+    // one surviving candidate per lane; its rank is the number of
+    // candidates better than it under the strict order, and the top_k
+    // ranks are kept
+    int base = 0;
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const bool pass = rf[t] > 0.0f && rf[t] >= cut;
+      const unsigned ball = __ballot_sync(0xffffffffu, pass);
+      if (pass) cj[base + __popc(ball & ((1u << lane) - 1u))] = lane + 32 * t;
+      base += __popc(ball);
+    }
+    __syncwarp();
+    const bool have = lane < npass;
+    RankKey mine;
+    mine.ratio = 0.0;
+    mine.pg = 0;
+    mine.lo = 0;
+    mine.hi = 0;
+    mine.j = -1;
+    if (have) {
+      const int j = cj[lane];
+      const long long pg = prow[j];
+      const int qj = q[j];
+      mine.j = j;
+      mine.ratio = ratio_of(j, pg);
+      mine.pg = pg;
+      mine.lo = qi < qj ? qi : qj;
+      mine.hi = qi < qj ? qj : qi;
+    }
+    int rank = 0;
+    for (int o = 0; o < npass; ++o) {
+      RankKey other;
+      other.ratio = __shfl_sync(0xffffffffu, mine.ratio, o);
+      other.pg = __shfl_sync(0xffffffffu, mine.pg, o);
+      other.lo = __shfl_sync(0xffffffffu, mine.lo, o);
+      other.hi = __shfl_sync(0xffffffffu, mine.hi, o);
+      if (have && o != lane && Better(other, mine)) ++rank;
+    }
+    if (have && rank < top_k) {
+      const int a = i < mine.j ? i : mine.j;
+      const int b = i < mine.j ? mine.j : i;
+      fmat[static_cast<long long>(a) * g + b] = 1;
+    }
+  } else {
+    // each lane keeps its best top_k candidates sorted, then the warp merges
+    // the 32 lists head by head (candidates are distinct, so no key ties)
+    RankKey lst[kLaneTopK];
+    int nl = 0;
+  #pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const int j = lane + 32 * t;
+      if (rf[t] <= 0.0f || rf[t] < cut) continue;
+      const long long pg = prow[j];
+      RankKey k;
+      k.j = j;
+      k.ratio = ratio_of(j, pg);
+      k.pg = pg;
+      const int qj = q[j];
+      k.lo = qi < qj ? qi : qj;
+      k.hi = qi < qj ? qj : qi;
+      if (nl == top_k && !Better(k, lst[nl - 1])) continue;
+      int pos = nl < top_k ? nl : top_k - 1;
+      while (pos > 0 && Better(k, lst[pos - 1])) {
+        lst[pos] = lst[pos - 1];
+        --pos;
+      }
+      lst[pos] = k;
+      if (nl < top_k) ++nl;
+    }
+    int head = 0;
+    for (int r = 0; r < top_k; ++r) {
+      RankKey best;
+      bool have = head < nl;
+      if (have) best = lst[head];
+      int src = lane;
+      for (int o = 16; o > 0; o >>= 1) {
+        RankKey other;
+        other.ratio = __shfl_xor_sync(0xffffffffu, best.ratio, o);
+        other.pg = __shfl_xor_sync(0xffffffffu, best.pg, o);
+        other.lo = __shfl_xor_sync(0xffffffffu, best.lo, o);
+        other.hi = __shfl_xor_sync(0xffffffffu, best.hi, o);
+        other.j = __shfl_xor_sync(0xffffffffu, best.j, o);
+        const int osrc = __shfl_xor_sync(0xffffffffu, src, o);
+        const int ohave = __shfl_xor_sync(0xffffffffu, have ? 1 : 0, o);
+        if (ohave && (!have || Better(other, best))) {
+          best = other;
+          have = true;
+          src = osrc;
+        }
+      }
+      if (!have) break;
+      if (src == lane) ++head;
+      if (lane == 0) {
+        const int a = i < best.j ? i : best.j;
+        const int b = i < best.j ? best.j : i;
+        fmat[static_cast<long long>(a) * g + b] = 1;
+      }
+    }
+  }
+}
+
 // Member pass of the big groups: one warp per member of every group in the
 // launch's big-group list (moff = prefix of the member counts), so a large
 // group's members are ranked by the whole GPU instead of one CTA.
@@ -979,144 +1130,18 @@ __global__ void __launch_bounds__(256) PrepareMembersKernel(PrepareParams P) {
       fmat[static_cast<long long>(a) * g + b] = 1;
     }
   } else if (top_k <= kLaneTopK) {
-    // fp32 prescreen: the exact (double) ratio is only computed for the
-    // candidates that can be in the member's top_k. The fp32 ratio of a
-    // candidate is within relative 3 * 2^-24 of its double ratio, so every
-    // candidate of the exact top_k has an fp32 ratio >= tau * (1 - 2^-20),
-    // where tau is the top_k-th largest fp32 ratio (found by bisection on the
-    // float bit patterns, which order like the positive values).
-    float rf[kMaxGroup / 32];
-#pragma unroll
-    for (int t = 0; t < kMaxGroup / 32; ++t) {
-      const int j = lane + 32 * t;
-      float v = 0.0f;  // not a candidate
-      if (j < g && j != i) {
-        const long long pg = prow[j];
-        if (pg > 0) {
-          long long denom = old_i + old[j];
-          if (denom < 1) denom = 1;
-          v = __fdiv_rn(static_cast<float>(pg), static_cast<float>(denom));
-        }
-      }
-      rf[t] = v;
-    }
-    float cut = 0.0f;
-    if (cnt > top_k + 16) {
-      unsigned lo = 0, hi = 0x7f800000u;  // count(bits >= lo) >= top_k > count(bits >= hi)
-      while (hi - lo > 1) {
-        const unsigned mid = lo + ((hi - lo) >> 1);
-        int c = 0;
-#pragma unroll
-        for (int t = 0; t < kMaxGroup / 32; ++t) c += __float_as_uint(rf[t]) >= mid ? 1 : 0;
-        c = WarpSumInt(c);
-        if (c >= top_k) lo = mid; else hi = mid;
-      }
-      cut = __uint_as_float(lo) * (1.0f - 9.5367431640625e-7f);
-    }
-    int npass = 0;
-#pragma unroll
-    for (int t = 0; t < kMaxGroup / 32; ++t) npass += (rf[t] > 0.0f && rf[t] >= cut) ? 1 : 0;
-    npass = WarpSumInt(npass);
-    if (npass <= 32) {
-      // one surviving candidate per lane; its rank is the number of
-      // candidates better than it under the strict order, and the top_k
-      // ranks are kept
-      int* cj = cand_j[threadIdx.x >> 5];
-      int base = 0;
-#pragma unroll
-      for (int t = 0; t < kMaxGroup / 32; ++t) {
-        const bool pass = rf[t] > 0.0f && rf[t] >= cut;
-        const unsigned ball = __ballot_sync(0xffffffffu, pass);
-        if (pass) cj[base + __popc(ball & ((1u << lane) - 1u))] = lane + 32 * t;
-        base += __popc(ball);
-      }
-      __syncwarp();
-      const bool have = lane < npass;
-      RankKey mine;
-      mine.ratio = 0.0;
-      mine.pg = 0;
-      mine.lo = 0;
-      mine.hi = 0;
-      mine.j = -1;
-      if (have) {
-        const int j = cj[lane];
-        const long long pg = prow[j];
-        const int qj = q[j];
-        mine.j = j;
-        mine.ratio = ratio_of(j, pg);
-        mine.pg = pg;
-        mine.lo = qi < qj ? qi : qj;
-        mine.hi = qi < qj ? qj : qi;
-      }
-      int rank = 0;
-      for (int o = 0; o < npass; ++o) {
-        RankKey other;
-        other.ratio = __shfl_sync(0xffffffffu, mine.ratio, o);
-        other.pg = __shfl_sync(0xffffffffu, mine.pg, o);
-        other.lo = __shfl_sync(0xffffffffu, mine.lo, o);
-        other.hi = __shfl_sync(0xffffffffu, mine.hi, o);
-        if (have && o != lane && Better(other, mine)) ++rank;
-      }
-      if (have && rank < top_k) {
-        const int a = i < mine.j ? i : mine.j;
-        const int b = i < mine.j ? mine.j : i;
-        fmat[static_cast<long long>(a) * g + b] = 1;
-      }
+    int* cj = cand_j[threadIdx.x >> 5];
+    const int nt = (g + 31) >> 5;
+    if (nt <= 1) {
+      MembersTopK<1>(lane, g, i, qi, top_k, cnt, prow, old, old_i, q, cj, fmat);
+    } else if (nt <= 2) {
+      MembersTopK<2>(lane, g, i, qi, top_k, cnt, prow, old, old_i, q, cj, fmat);
+    } else if (nt <= 4) {
+      MembersTopK<4>(lane, g, i, qi, top_k, cnt, prow, old, old_i, q, cj, fmat);
+    } else if (nt <= 8) {
+      MembersTopK<8>(lane, g, i, qi, top_k, cnt, prow, old, old_i, q, cj, fmat);
     } else {
-    // each lane keeps its best top_k candidates sorted, then the warp merges
-    // the 32 lists head by head (candidates are distinct, so no key ties)
-    RankKey lst[kLaneTopK];
-    int nl = 0;
-#pragma unroll
-    for (int t = 0; t < kMaxGroup / 32; ++t) {
-      const int j = lane + 32 * t;
-      if (rf[t] <= 0.0f || rf[t] < cut) continue;
-      const long long pg = prow[j];
-      RankKey k;
-      k.j = j;
-      k.ratio = ratio_of(j, pg);
-      k.pg = pg;
-      const int qj = q[j];
-      k.lo = qi < qj ? qi : qj;
-      k.hi = qi < qj ? qj : qi;
-      if (nl == top_k && !Better(k, lst[nl - 1])) continue;
-      int pos = nl < top_k ? nl : top_k - 1;
-      while (pos > 0 && Better(k, lst[pos - 1])) {
-        lst[pos] = lst[pos - 1];
-        --pos;
-      }
-      lst[pos] = k;
-      if (nl < top_k) ++nl;
-    }
-    int head = 0;
-    for (int r = 0; r < top_k; ++r) {
-      RankKey best;
-      bool have = head < nl;
-      if (have) best = lst[head];
-      int src = lane;
-      for (int o = 16; o > 0; o >>= 1) {
-        RankKey other;
-        other.ratio = __shfl_xor_sync(0xffffffffu, best.ratio, o);
-        other.pg = __shfl_xor_sync(0xffffffffu, best.pg, o);
-        other.lo = __shfl_xor_sync(0xffffffffu, best.lo, o);
-        other.hi = __shfl_xor_sync(0xffffffffu, best.hi, o);
-        other.j = __shfl_xor_sync(0xffffffffu, best.j, o);
-        const int osrc = __shfl_xor_sync(0xffffffffu, src, o);
-        const int ohave = __shfl_xor_sync(0xffffffffu, have ? 1 : 0, o);
-        if (ohave && (!have || Better(other, best))) {
-          best = other;
-          have = true;
-          src = osrc;
-        }
-      }
-      if (!have) break;
-      if (src == lane) ++head;
-      if (lane == 0) {
-        const int a = i < best.j ? i : best.j;
-        const int b = i < best.j ? best.j : i;
-        fmat[static_cast<long long>(a) * g + b] = 1;
-      }
-    }
+      MembersTopK<kMaxGroup / 32>(lane, g, i, qi, top_k, cnt, prow, old, old_i, q, cj, fmat);
     }
   } else {
     RankKey prev;
