@@ -2321,44 +2321,73 @@ __device__ int RewriteRow(const CommitParams& P, Entry* S, int L, int* D, Entry*
     nins = 0;
     carry = 0;
   }
-  for (int i = tid; i < L; i += kRowsThreads) {
-    int drop = 0;
-    if (i > 0 && EntNb(S[i]) == EntNb(S[i - 1])) {
-      atomicAdd(reinterpret_cast<unsigned long long*>(&S[i - 1]), static_cast<unsigned long long>(EntCnt(S[i])));
-      drop = 1;
+  if (sk >= 0) {
+    // a keep row staged as the merge of two rows: equal neighbours are adjacent
+    for (int i = tid; i < L; i += kRowsThreads) {
+      int drop = 0;
+      if (i > 0 && EntNb(S[i]) == EntNb(S[i - 1])) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(&S[i - 1]), static_cast<unsigned long long>(EntCnt(S[i])));
+        drop = 1;
+      }
+      D[i] = drop;
     }
-    D[i] = drop;
+  } else {
+    // a neighbour row is canonical
+    for (int i = tid; i < L; i += kRowsThreads) D[i] = 0;
   }
   __syncthreads();
-  for (int i = tid; i < L; i += kRowsThreads) {
-    if (D[i]) continue;
-    const int id = EntNb(S[i]);
-    if (id == sk || id == sr) {
-      D[i] = 1;
-      continue;
+  // entries of supernodes removed in this block: four lookups in flight per
+  // thread
+  for (int i0 = tid; i0 < L; i0 += 4 * kRowsThreads) {
+    int id[4], st[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * kRowsThreads;
+      id[u] = i < L && !D[i] ? EntNb(S[i]) : -1;
     }
-    if (P.stamp[id] == remove_stamp) {
-      const int kp = P.partner[id];
-      D[i] = 1;
-      if (kp == sk) continue;
-      const int p = RowLowerBound(S, L, kp);
-      const long long c = EntCnt(S[i]);
-      if (p < L && EntNb(S[p]) == kp) {
-        atomicAdd(reinterpret_cast<unsigned long long*>(&S[p]), static_cast<unsigned long long>(c));
-      } else {
-        INS[atomicAdd(&nins, 1)] = MakeEnt(kp, c);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) st[u] = id[u] >= 0 && id[u] != sk && id[u] != sr ? P.stamp[id[u]] : 0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int i = i0 + u * kRowsThreads;
+      if (id[u] < 0) continue;
+      if (id[u] == sk || id[u] == sr) {
+        D[i] = 1;
+        continue;
+      }
+      if (st[u] == remove_stamp) {
+        const int kp = P.partner[id[u]];
+        D[i] = 1;
+        if (kp == sk) continue;
+        const int p = RowLowerBound(S, L, kp);
+        const long long c = EntCnt(S[i]);
+        if (p < L && EntNb(S[p]) == kp) {
+          atomicAdd(reinterpret_cast<unsigned long long*>(&S[p]), static_cast<unsigned long long>(c));
+        } else {
+          INS[atomicAdd(&nins, 1)] = MakeEnt(kp, c);
+        }
       }
     }
   }
   __syncthreads();
-  // exclusive scan of drop flags (D[L] = total)
-  for (int base = 0; base < L; base += kRowsThreads) {
-    const int i = base + tid;
-    const int v = i < L ? D[i] : 0;
+  // exclusive scan of drop flags (D[L] = total), four flags per thread a step
+  for (int base = 0; base < L; base += 4 * kRowsThreads) {
+    const int i0 = base + 4 * tid;
+    int v[4], sum = 0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      v[u] = i0 + u < L ? D[i0 + u] : 0;
+      sum += v[u];
+    }
     int ex = 0, agg = 0;
-    BlockScan(scan_tmp).ExclusiveSum(v, ex, agg);
+    BlockScan(scan_tmp).ExclusiveSum(sum, ex, agg);
     __syncthreads();
-    if (i < L) D[i] = carry + ex;
+    int run = carry + ex;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (i0 + u < L) D[i0 + u] = run;
+      run += v[u];
+    }
     __syncthreads();
     if (tid == 0) carry += agg;
     __syncthreads();
