@@ -2805,12 +2805,18 @@ constexpr int kPlanItems = 8;
 constexpr int kPlanTile = kPlanThreads * kPlanItems;
 enum PlanScalar : int {
   kPlanR = 0, kPlanCand, kPlanSel, kPlanSmall, kPlanBig, kPlanMembers, kPlanSlots, kPlanMat, kPlanMaxE,
-  kPlanSelSmall, kPlanSelMid, kPlanSelBig, kPlanScalars
+  kPlanSelSmall, kPlanSelMid, kPlanSelBig, kPlanSmallBase, kPlanScalars = kPlanSmallBase + 4
 };
+// The small-group list is laid out by member count, largest class first
+// (more than 24, 17..24, 9..16, at most 8 members): the longest warps start
+// first instead of forming the prepare kernel's tail.
+constexpr int kPlanSmallClasses = 4;
+__device__ __forceinline__ int SmallClass(int g) { return g > 24 ? 0 : g > 16 ? 1 : g > 8 ? 2 : 3; }
 
 struct PlanSums {
   long long cand, sel, moff, soff, mat;
-  int real, small, big, ssmall, smid, sbig;
+  int real, big, ssmall, smid, sbig;
+  int small[kPlanSmallClasses];
 };
 
 struct PlanSumOp {
@@ -2822,7 +2828,8 @@ struct PlanSumOp {
     r.soff = a.soff + b.soff;
     r.mat = a.mat + b.mat;
     r.real = a.real + b.real;
-    r.small = a.small + b.small;
+#pragma unroll
+    for (int c = 0; c < kPlanSmallClasses; ++c) r.small[c] = a.small[c] + b.small[c];
     r.big = a.big + b.big;
     r.ssmall = a.ssmall + b.ssmall;
     r.smid = a.smid + b.smid;
@@ -2834,7 +2841,9 @@ struct PlanSumOp {
 __device__ __forceinline__ PlanSums PlanZero() {
   PlanSums z;
   z.cand = z.sel = z.moff = z.soff = z.mat = 0;
-  z.real = z.small = z.big = z.ssmall = z.smid = z.sbig = 0;
+  z.real = z.big = z.ssmall = z.smid = z.sbig = 0;
+#pragma unroll
+  for (int c = 0; c < kPlanSmallClasses; ++c) z.small[c] = 0;
   return z;
 }
 
@@ -2847,7 +2856,7 @@ __device__ __forceinline__ PlanSums PlanOfGroup(int g, unsigned e, long long k) 
   f.cand = gl * (gl - 1) / 2 < gl * k ? gl * (gl - 1) / 2 : gl * k;
   f.sel = gl / 2;
   if (g <= kSmallGroup && e <= static_cast<unsigned>(kSmallStage)) {
-    f.small = 1;
+    f.small[SmallClass(g)] = 1;
   } else {
     f.big = 1;
     f.moff = gl;
@@ -2931,7 +2940,12 @@ __global__ void __launch_bounds__(kPlanThreads) PlanScanKernel(PlanParams P) {
     s[kPlanR] = T.real;
     s[kPlanCand] = T.cand;
     s[kPlanSel] = T.sel;
-    s[kPlanSmall] = T.small;
+    long long sb = 0;
+    for (int c = 0; c < kPlanSmallClasses; ++c) {
+      s[kPlanSmallBase + c] = sb;
+      sb += T.small[c];
+    }
+    s[kPlanSmall] = sb;
     s[kPlanBig] = T.big;
     s[kPlanMembers] = T.moff;
     s[kPlanSlots] = T.soff;
@@ -2972,8 +2986,9 @@ __global__ void __launch_bounds__(kPlanThreads) PlanScatterKernel(PlanParams P) 
       P.cand_off[ri] = off.cand;
       P.sel_off[ri] = off.sel;
       P.mat_off[ri] = f.big ? off.mat : 0;
-      if (f.small) {
-        P.small[off.small] = ri;
+      if (!f.big) {
+        const int c = SmallClass(g[j]);
+        P.small[P.scalars[kPlanSmallBase + c] + off.small[c]] = ri;
       } else {
         P.big[off.big] = ri;
         P.big_moff[off.big] = off.moff;
