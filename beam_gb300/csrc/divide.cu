@@ -196,6 +196,79 @@ __global__ void GatherSortedKernel(const int* __restrict__ perm, int items, cons
   }
 }
 
+// The radix sort orders the items by the high 32 bits of their keys only
+// (half the passes); items with equal high words stay in input order. Where
+// such a run mixes low words it is put in full-key order below, which gives
+// the order of a stable sort by the whole key. Such runs need two distinct
+// 64-bit hashes with equal high words, so they are few and short.
+// First pass (keys are only read): the first position of each run where the
+// low word changes records the run's start.
+__global__ void MixedRunsKernel(const unsigned long long* __restrict__ keys, const int* __restrict__ item_seg,
+                                const int* __restrict__ ubeg, int items, int* __restrict__ list,
+                                int* __restrict__ cnt) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x + 1; j < items; j += gridDim.x * blockDim.x) {
+    const unsigned long long kj = keys[j];
+    const unsigned long long kp = keys[j - 1];
+    if (kj == kp || (kj >> 32) != (kp >> 32)) continue;
+    const int sg = item_seg[j];
+    if (item_seg[j - 1] != sg) continue;
+    const int b = ubeg[sg];
+    const unsigned long long hi = kj >> 32;
+    int r0 = j - 1;
+    bool first = true;
+    while (r0 > b && (keys[r0 - 1] >> 32) == hi) {
+      if (keys[r0 - 1] != keys[r0]) {
+        first = false;  // an earlier change records this run
+        break;
+      }
+      --r0;
+    }
+    if (first) list[atomicAdd(cnt, 1)] = r0;
+  }
+}
+
+// Second pass, one CTA: each recorded run is reordered stably by its keys
+// (the items of the smallest remaining key move first, in their order) via
+// the scratch arrays; the run counter is cleared for the next sort.
+__global__ void SortMixedRunsKernel(unsigned long long* __restrict__ keys, int* __restrict__ vals,
+                                    const int* __restrict__ item_seg, const int* __restrict__ uend,
+                                    const int* __restrict__ list, int* __restrict__ cnt,
+                                    unsigned long long* __restrict__ tk, int* __restrict__ tv) {
+  const int nruns = *cnt;
+  for (int t = threadIdx.x; t < nruns; t += blockDim.x) {
+    const int r0 = list[t];
+    const unsigned long long hi = keys[r0] >> 32;
+    const int e = uend[item_seg[r0]];
+    int r1 = r0 + 1;
+    while (r1 < e && (keys[r1] >> 32) == hi) ++r1;
+    int w = r0;
+    unsigned long long last = 0;
+    bool any = false;
+    while (w < r1) {
+      unsigned long long mn = ~0ull;
+      for (int i = r0; i < r1; ++i) {
+        const unsigned long long k = keys[i];
+        if ((!any || k > last) && k < mn) mn = k;
+      }
+      for (int i = r0; i < r1; ++i) {
+        if (keys[i] == mn) {
+          tk[w] = mn;
+          tv[w] = vals[i];
+          ++w;
+        }
+      }
+      last = mn;
+      any = true;
+    }
+    for (int i = r0; i < r1; ++i) {
+      keys[i] = tk[i];
+      vals[i] = tv[i];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *cnt = 0;
+}
+
 __global__ void ScatterSortedKernel(const int* __restrict__ pos_map, const int* __restrict__ item_seg,
                                     const int* __restrict__ ubeg, int items,
                                     const unsigned long long* __restrict__ keys, const int* __restrict__ vals,
@@ -259,6 +332,9 @@ void Engine::Divide(int iter) {
   int* uend = ubeg + n;
   int* seg_start = d_seg_beg_.p;
   int* item_seg = d_seg_end_.p;
+  int* fix_cnt = uend + n + 8;  // mixed-run counter (cleared by each second pass)
+  d_fix_list_.ensure(static_cast<size_t>(n) + 1);
+  CheckCuda(cudaMemsetAsync(fix_cnt, 0, sizeof(int), s), "memset mixed-run counter");
 
   auto scan_excl = [&](const int* in, int* out, int items) {
     size_t bytes = 0;
@@ -371,11 +447,12 @@ void Engine::Divide(int iter) {
       ++launches_;
       IotaKernel<<<Blocks(items, T), T, 0, s>>>(d_perm_.p, items);
       size_t bytes = 0;
+      // by the high key words (equal-high runs are put in key order below)
       CheckCuda(cub::DeviceRadixSort::SortPairs(nullptr, bytes, d_keys_.p, d_keys_alt_.p, d_perm_.p, d_perm_alt_.p,
-                                                items, 0, 64, s), "cub radix sort size");
+                                                items, 32, 64, s), "cub radix sort size");
       d_cub_tmp_.ensure(bytes);
       CheckCuda(cub::DeviceRadixSort::SortPairs(d_cub_tmp_.p, bytes, d_keys_.p, d_keys_alt_.p, d_perm_.p,
-                                                d_perm_alt_.p, items, 0, 64, s), "cub radix sort");
+                                                d_perm_alt_.p, items, 32, 64, s), "cub radix sort");
       int* perm = d_perm_alt_.p;
       if (nu > 1) {
         int bits = 1;
@@ -393,6 +470,13 @@ void Engine::Divide(int iter) {
       ++launches_;
       GatherSortedKernel<<<Blocks(items, T), T, 0, s>>>(perm, items, d_keys_.p, d_vals_.p, d_keys_alt_.p,
                                                         d_vals_alt_.p);
+      // runs of equal high words with mixed low words into full-key order
+      // (d_keys_ / d_vals_ are free once gathered)
+      ++launches_;
+      MixedRunsKernel<<<Blocks(items, T), T, 0, s>>>(d_keys_alt_.p, item_seg, ubeg, items, d_fix_list_.p, fix_cnt);
+      ++launches_;
+      SortMixedRunsKernel<<<1, T, 0, s>>>(d_keys_alt_.p, d_vals_alt_.p, item_seg, uend, d_fix_list_.p, fix_cnt,
+                                          d_keys_.p, d_vals_.p);
       ++launches_;
       ScatterSortedKernel<<<Blocks(items, T), T, 0, s>>>(d_pos_map_.p, item_seg, ubeg, items, d_keys_alt_.p,
                                                          d_vals_alt_.p, fallback ? 1 : 0, cfg_.divide_max_group,
