@@ -867,14 +867,28 @@ __device__ __forceinline__ void AccumPair(const RunEntry& a, const RunEntry& b, 
   }
 }
 
+// kAccumSplit warps share a chunk: warp y pairs the chunk with the earlier
+// chunks y + 1, y + 1 + kAccumSplit, ... of its run (warp 0 also within the
+// chunk), so a chunk deep in a long run is not one warp's long loop.
+constexpr int kAccumSplit = 4;
+
 __global__ void __launch_bounds__(kAccumThreads) PrepareAccumKernel(PrepareParams P) {
   const int lane = threadIdx.x & 31;
   unsigned long long examined = 0;
   const long long nchunks = (P.nslots + 31) >> 5;
+  const long long nwork = nchunks * kAccumSplit;
   const long long wstride = static_cast<long long>(gridDim.x) * (kAccumThreads / 32);
-  for (long long ch = (static_cast<long long>(blockIdx.x) * kAccumThreads + threadIdx.x) >> 5; ch < nchunks;
-       ch += wstride) {
+  for (long long wk = (static_cast<long long>(blockIdx.x) * kAccumThreads + threadIdx.x) >> 5; wk < nwork;
+       wk += wstride) {
+    const long long ch = wk / kAccumSplit;
+    const int y = static_cast<int>(wk % kAccumSplit);
     const long long p0 = ch << 5;
+    if (y > 0) {
+      // nothing unless the chunk's first run reaches back at least y + 1 chunks
+      if (p0 < 32ll * (y + 1)) continue;
+      const unsigned long long f = P.skey_sorted[p0];
+      if (f == kSlotPad || P.skey_sorted[p0 - 32ll * y - 1] != f) continue;
+    }
     const long long p = p0 + lane;
     RunEntry me;
     me.key = p < P.nslots ? P.skey_sorted[p] : kSlotPad;
@@ -898,9 +912,11 @@ __global__ void __launch_bounds__(kAccumThreads) PrepareAccumKernel(PrepareParam
       st = P.Q.size[t];
     }
     // pairs inside the chunk
-    for (int src = 0; src < 31; ++src) {
-      const RunEntry o = ShflRunEntry(me, src);
-      if (valid && src < lane && o.key == me.key) AccumPair(me, o, t, st, g, pmat, examined);
+    if (y == 0) {
+      for (int src = 0; src < 31; ++src) {
+        const RunEntry o = ShflRunEntry(me, src);
+        if (valid && src < lane && o.key == me.key) AccumPair(me, o, t, st, g, pmat, examined);
+      }
     }
     // the run holding the chunk's first slot may start in earlier chunks
     const unsigned long long first = __shfl_sync(0xffffffffu, me.key, 0);
@@ -910,8 +926,9 @@ __global__ void __launch_bounds__(kAccumThreads) PrepareAccumKernel(PrepareParam
     const int fg = P.glen[P.real[P.list[P.list0 + fbl]]];
     const DeferredView FV = Deferred(P.desc[P.list0 + fbl].base, fg);
     const bool mine = valid && me.key == first;
-    for (long long c0 = p0 - 32;; c0 -= 32) {
-      // c0 >= 0: p0 is a multiple of 32 and slot p0 - 1 is in the run
+    for (long long c0 = p0 - 32ll * (y + 1);; c0 -= 32ll * kAccumSplit) {
+      // c0 >= 0; the chunk holds run entries iff its last slot is in the run
+      if (P.skey_sorted[c0 + 31] != first) break;
       RunEntry o;
       o.key = P.skey_sorted[c0 + lane];
       o.c = o.s = 0;
@@ -921,7 +938,8 @@ __global__ void __launch_bounds__(kAccumThreads) PrepareAccumKernel(PrepareParam
         const RunEntry b = ShflRunEntry(o, src);
         if (mine && b.key == first) AccumPair(me, b, t, st, g, pmat, examined);
       }
-      if (c0 == 0 || __shfl_sync(0xffffffffu, o.key, 0) != first) break;
+      // the run continues below this chunk iff its first slot is in the run
+      if (c0 < 32ll * kAccumSplit || __shfl_sync(0xffffffffu, o.key, 0) != first) break;
     }
   }
   examined = static_cast<unsigned long long>(WarpSum(static_cast<long long>(examined)));
@@ -3444,7 +3462,7 @@ void Engine::LaunchPrepare(const BlockPlan& bp) {
       d_cub_tmp_.ensure(bytes);
       CheckCuda(cub::DeviceRadixSort::SortPairs(d_cub_tmp_.p, bytes, d_skey_[0].p, d_skey_[1].p, d_sval_[0].p,
                                                 d_sval_[1].p, PP.nslots, 0, bits, stream_), "cub radix sort");
-      const long long want = ((PP.nslots + 31) / 32 + kAccumThreads / 32 - 1) / (kAccumThreads / 32);
+      const long long want = ((PP.nslots + 31) / 32 * kAccumSplit + kAccumThreads / 32 - 1) / (kAccumThreads / 32);
       ++launches_;
       PrepareAccumKernel<<<static_cast<int>(std::min(want, 152ll * 16)), kAccumThreads, 0, stream_>>>(PP);
     }
