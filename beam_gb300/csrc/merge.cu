@@ -39,7 +39,7 @@ constexpr int kSmemHeads = 4096;     // bucket hash heads in shared memory
 // even when their rows fit the shared-memory table: the pairs of members
 // sharing a target grow with the square of the member count, too much work
 // for one CTA.
-constexpr int kSmemMaxGroup = 64;
+constexpr int kSmemMaxGroup = 48;
 constexpr int kScoreThreads = 256;
 constexpr int kFewGroups = 256;  // blocks of at most this many groups take fewer, wider launches
 constexpr int kSelectMidGroup = 32;   // groups of 9..32 members: a small CTA each
@@ -150,10 +150,11 @@ __device__ void WarpExactGain(const QuotientView& Q, int a, int b, long long* ga
   }
   before = WarpSum(before);
   after = WarpSum(after);
-  eab_a = WarpMax(eab_a);
-  eab_b = WarpMax(eab_b);
-  uni = WarpSumInt(uni);
-  ovl = WarpSumInt(ovl);
+  // e(a,b) is read by one lane per row (counts < 2^32)
+  eab_a = __reduce_max_sync(kFull, static_cast<unsigned>(eab_a));
+  eab_b = __reduce_max_sync(kFull, static_cast<unsigned>(eab_b));
+  uni = static_cast<int>(__reduce_add_sync(kFull, static_cast<unsigned>(uni)));
+  ovl = static_cast<int>(__reduce_add_sync(kFull, static_cast<unsigned>(ovl)));
   bad = __any_sync(kFull, bad);
   if (eab_a != eab_b) {
     if (lane == 0) RaiseError(err, kErrAsymmetric, a, b, 0);
@@ -345,12 +346,11 @@ __device__ void WarpExactGainShared(const QuotientView& Q, const RowConsts& RC, 
       (on_a ? heavy_a : heavy_b) = term;
     }
   }
-  shared = WarpSum(shared);
-  heavy_a = WarpSum(heavy_a);
-  heavy_b = WarpSum(heavy_b);
-  eab_a = WarpMax(eab_a);
-  eab_b = WarpMax(eab_b);
-  ovl = WarpSumInt(ovl);
+  // one 64-bit sum; e(a,b) is read by one lane per row (counts < 2^32)
+  shared = WarpSum(shared + heavy_a + heavy_b);
+  eab_a = __reduce_max_sync(kFull, static_cast<unsigned>(eab_a));
+  eab_b = __reduce_max_sync(kFull, static_cast<unsigned>(eab_b));
+  ovl = static_cast<int>(__reduce_add_sync(kFull, static_cast<unsigned>(ovl)));
   bad = __any_sync(kFull, bad);
   if (eab_a != eab_b) {
     if (lane == 0) RaiseError(err, kErrAsymmetric, a, b, 0);
@@ -359,7 +359,7 @@ __device__ void WarpExactGainShared(const QuotientView& Q, const RowConsts& RC, 
   const long long ib = Q.internal[b];
   const long long before = RC.before[a] + RC.before[b] - BlockCost(sb, sa, eab_b, false, bad) +
                            BlockCost(sa, sa, ia, true, bad) + BlockCost(sb, sb, ib, true, bad);
-  const long long after = RC.light[a] + heavy_a + RC.light[b] + heavy_b - BlockCost(sw, sb, eab_a, false, bad) -
+  const long long after = RC.light[a] + RC.light[b] - BlockCost(sw, sb, eab_a, false, bad) -
                           BlockCost(sw, sa, eab_b, false, bad) + shared +
                           BlockCost(sw, sw, ia + ib + eab_a, true, bad);
   if (bad && lane == 0) RaiseError(err, kErrBlockCost, a, b, 0);
