@@ -1992,8 +1992,10 @@ __device__ __forceinline__ void SelectMatchGroup(const SelectParams& P, int ri) 
     nkeys = 0;
     nchosen = 0;
     rej_thr = 0;
-    gkeys = cnt <= kMatchSmemKeys ? skeys
-                                  : ScratchAlloc(P.scratch, P.scratch_cap, P.ctl, 8ull * cnt, P.err);
+    // two key buffers of cnt entries: the live keys are compacted from one
+    // into the other every round
+    gkeys = 2 * cnt <= kMatchSmemKeys ? skeys
+                                      : ScratchAlloc(P.scratch, P.scratch_cap, P.ctl, 16ull * cnt, P.err);
   }
   for (int i = tid; i < g; i += kMatchThreads) matched[i] = 0;
   __syncthreads();
@@ -2028,21 +2030,24 @@ __device__ __forceinline__ void SelectMatchGroup(const SelectParams& P, int ri) 
   const int m = nkeys;
   const unsigned long long idx_mask = (1ull << kKeyIdxBits) - 1;
   // rounds of locally dominant keys (each round selects at least the
-  // smallest live key, so at most g/2 rounds)
-  for (int round = 0; round <= kMaxGroup / 2; ++round) {
+  // smallest live key, so at most g/2 rounds); the keys still live after a
+  // round move to the other buffer (the matching depends on the key values
+  // only, not on their order)
+  unsigned long long* kin = keys;
+  unsigned long long* kout = keys + cnt;
+  int nlive = m;
+  for (int round = 0; round <= kMaxGroup / 2 && nlive > 0; ++round) {
     for (int i = tid; i < g; i += kMatchThreads) best[i] = ~0ull;
     if (tid == 0) live_any = 0;
     __syncthreads();
-    for (int k = tid; k < m; k += kMatchThreads) {
-      const unsigned long long key = keys[k];
-      if (key == ~0ull) continue;
+    for (int k = tid; k < nlive; k += kMatchThreads) {
+      const unsigned long long key = kin[k];
       atomicMin(&best[(key >> kKeyIdxBits) & idx_mask], key);
       atomicMin(&best[key & idx_mask], key);
     }
     __syncthreads();
-    for (int k = tid; k < m; k += kMatchThreads) {
-      const unsigned long long key = keys[k];
-      if (key == ~0ull) continue;
+    for (int k = tid; k < nlive; k += kMatchThreads) {
+      const unsigned long long key = kin[k];
       const int a = static_cast<int>((key >> kKeyIdxBits) & idx_mask);
       const int b = static_cast<int>(key & idx_mask);
       if (best[a] == key && best[b] == key) {
@@ -2052,17 +2057,18 @@ __device__ __forceinline__ void SelectMatchGroup(const SelectParams& P, int ri) 
       }
     }
     __syncthreads();
-    for (int k = tid; k < m; k += kMatchThreads) {
-      const unsigned long long key = keys[k];
-      if (key == ~0ull) continue;
-      if (matched[(key >> kKeyIdxBits) & idx_mask] || matched[key & idx_mask]) {
-        keys[k] = ~0ull;
-      } else {
-        live_any = 1;
+    for (int k = tid; k < nlive; k += kMatchThreads) {
+      const unsigned long long key = kin[k];
+      if (!matched[(key >> kKeyIdxBits) & idx_mask] && !matched[key & idx_mask]) {
+        kout[atomicAdd(&live_any, 1)] = key;
       }
     }
     __syncthreads();
-    if (!live_any) break;
+    nlive = live_any;
+    unsigned long long* t = kin;
+    kin = kout;
+    kout = t;
+    __syncthreads();  // every thread has read live_any before the next round resets it
   }
   // the selected keys in greedy (ascending key) order
   const int ns = nchosen;
