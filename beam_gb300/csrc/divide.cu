@@ -91,6 +91,27 @@ __global__ void SegLenAllKernel(const int* __restrict__ seg_start, const int* __
 }
 
 // {segments, unfinished segments, their items} of a depth, for one read-back.
+// Depth 0: one segment of all `count` active supernodes (only position 0
+// carries a head flag). Writes what the scans and SegStarts / SegLenAll
+// would: every item's inclusive head count is 1, and segment 0's start,
+// length, unfinished flag and item count with both exclusive offsets 0.
+__global__ void DepthZeroKernel(int count, int max_group, int* __restrict__ incl, int* __restrict__ seg_start,
+                                int* __restrict__ seg_len, int* __restrict__ unf_flag, int* __restrict__ unf_len,
+                                int* __restrict__ unf_idx, int* __restrict__ unf_off) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= count) return;
+  incl[p] = 1;
+  if (p == 0) {
+    const int unf = count > max_group ? 1 : 0;
+    seg_start[0] = 0;
+    seg_len[0] = count;
+    unf_flag[0] = unf;
+    unf_len[0] = unf ? count : 0;
+    unf_idx[0] = 0;
+    unf_off[0] = 0;
+  }
+}
+
 __global__ void DepthCountsKernel(const int* __restrict__ incl_last, const int* __restrict__ unf_idx_last,
                                   const int* __restrict__ unf_flag_last, const int* __restrict__ unf_off_last,
                                   const int* __restrict__ unf_len_last, int* __restrict__ out) {
@@ -391,14 +412,20 @@ void Engine::Divide(int iter) {
     bool settled = false;  // the loop ended with segs / seg_start / seg_len of the final groups
     for (int depth = 0; depth <= cfg_.divide_hash_dims; ++depth) {
       const bool fallback = depth == cfg_.divide_hash_dims;
-      scan_incl(d_head_flag_.p, scan, count);
-      ++launches_;
-      SegStartsKernel<<<Blocks(count, T), T, 0, s>>>(d_head_flag_.p, scan, count, seg_start);
-      ++launches_;
-      SegLenAllKernel<<<Blocks(count, T), T, 0, s>>>(seg_start, scan + count - 1, count, cfg_.divide_max_group,
-                                                     seg_len, unf_flag, unf_len);
-      scan_excl(unf_flag, unf_idx, count);
-      scan_excl(unf_len, unf_off, count);
+      if (depth == 0) {
+        ++launches_;
+        DepthZeroKernel<<<Blocks(count, T), T, 0, s>>>(count, cfg_.divide_max_group, scan, seg_start, seg_len,
+                                                       unf_flag, unf_len, unf_idx, unf_off);
+      } else {
+        scan_incl(d_head_flag_.p, scan, count);
+        ++launches_;
+        SegStartsKernel<<<Blocks(count, T), T, 0, s>>>(d_head_flag_.p, scan, count, seg_start);
+        ++launches_;
+        SegLenAllKernel<<<Blocks(count, T), T, 0, s>>>(seg_start, scan + count - 1, count, cfg_.divide_max_group,
+                                                       seg_len, unf_flag, unf_len);
+        scan_excl(unf_flag, unf_idx, count);
+        scan_excl(unf_len, unf_off, count);
+      }
       // segments, unfinished segments and their items: known on the host at
       // depth 0 (one segment of all active supernodes), one read-back later
       int hc[3];
