@@ -187,11 +187,14 @@ __global__ void MinHashKernel(const int* __restrict__ arc_src, const int* __rest
 
 __global__ void GatherKeysKernel(const int* __restrict__ order, const int* __restrict__ pos_map, int items,
                                  const unsigned long long* __restrict__ hash, int fallback, uint64_t seed,
-                                 int iter, unsigned long long* __restrict__ keys, int* __restrict__ vals) {
+                                 int iter, unsigned long long* __restrict__ keys, unsigned* __restrict__ keys_hi,
+                                 int* __restrict__ vals) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < items) {
     const int rep = order[pos_map[k]];
-    keys[k] = fallback ? FallbackRank(seed, rep, iter) : hash[rep];
+    const unsigned long long key = fallback ? FallbackRank(seed, rep, iter) : hash[rep];
+    keys[k] = key;
+    keys_hi[k] = static_cast<unsigned>(key >> 32);  // the radix sort's key
     vals[k] = rep;
   }
 }
@@ -355,6 +358,8 @@ void Engine::Divide(int iter) {
   int* item_seg = d_seg_end_.p;
   int* fix_cnt = uend + n + 8;  // mixed-run counter (cleared by each second pass)
   d_fix_list_.ensure(static_cast<size_t>(n) + 1);
+  d_keys_hi_[0].ensure(static_cast<size_t>(n) + 1);
+  d_keys_hi_[1].ensure(static_cast<size_t>(n) + 1);
   CheckCuda(cudaMemsetAsync(fix_cnt, 0, sizeof(int), s), "memset mixed-run counter");
 
   auto scan_excl = [&](const int* in, int* out, int items) {
@@ -468,18 +473,19 @@ void Engine::Divide(int iter) {
       }
       ++launches_;
       GatherKeysKernel<<<Blocks(items, T), T, 0, s>>>(d_order_.p, d_pos_map_.p, items, d_hash_.p, fallback ? 1 : 0,
-                                                      cfg_.seed, iter, d_keys_.p, d_vals_.p);
+                                                      cfg_.seed, iter, d_keys_.p, d_keys_hi_[0].p, d_vals_.p);
       // (segment, key) order, stable on the rep order inside each segment:
       // a stable LSD radix sort by key, then a stable one by segment index.
       ++launches_;
       IotaKernel<<<Blocks(items, T), T, 0, s>>>(d_perm_.p, items);
       size_t bytes = 0;
-      // by the high key words (equal-high runs are put in key order below)
-      CheckCuda(cub::DeviceRadixSort::SortPairs(nullptr, bytes, d_keys_.p, d_keys_alt_.p, d_perm_.p, d_perm_alt_.p,
-                                                items, 32, 64, s), "cub radix sort size");
+      // by the high key words (equal-high runs are put in key order below;
+      // the full keys follow the permutation in GatherSortedKernel)
+      CheckCuda(cub::DeviceRadixSort::SortPairs(nullptr, bytes, d_keys_hi_[0].p, d_keys_hi_[1].p, d_perm_.p,
+                                                d_perm_alt_.p, items, 0, 32, s), "cub radix sort size");
       d_cub_tmp_.ensure(bytes);
-      CheckCuda(cub::DeviceRadixSort::SortPairs(d_cub_tmp_.p, bytes, d_keys_.p, d_keys_alt_.p, d_perm_.p,
-                                                d_perm_alt_.p, items, 32, 64, s), "cub radix sort");
+      CheckCuda(cub::DeviceRadixSort::SortPairs(d_cub_tmp_.p, bytes, d_keys_hi_[0].p, d_keys_hi_[1].p, d_perm_.p,
+                                                d_perm_alt_.p, items, 0, 32, s), "cub radix sort");
       int* perm = d_perm_alt_.p;
       if (nu > 1) {
         int bits = 1;
