@@ -71,9 +71,12 @@ __global__ void SegLenKernel(const int* __restrict__ seg_start, int segs, int co
 // SegLenKernel over all count positions with the segment count read on the
 // device (no host round trip): entries past the last segment are zeroed, so
 // scans over count elements equal scans over the segments.
+// unf_pk[s] = unfinished flag << 32 | unfinished item count: one exclusive
+// scan gives both the unfinished-segment index (high word) and the compact
+// item offset (low word, < 2^31, so no carry reaches the high word).
 __global__ void SegLenAllKernel(const int* __restrict__ seg_start, const int* __restrict__ segs_p, int count,
                                 int max_group, int* __restrict__ seg_len, int* __restrict__ unf_flag,
-                                int* __restrict__ unf_len) {
+                                unsigned long long* __restrict__ unf_pk) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= count) return;
   const int segs = *segs_p;
@@ -83,10 +86,10 @@ __global__ void SegLenAllKernel(const int* __restrict__ seg_start, const int* __
     seg_len[s] = len;
     const int unf = len > max_group ? 1 : 0;
     unf_flag[s] = unf;
-    unf_len[s] = unf ? len : 0;
+    unf_pk[s] = unf ? (1ull << 32) | static_cast<unsigned>(len) : 0ull;
   } else {
     unf_flag[s] = 0;
-    unf_len[s] = 0;
+    unf_pk[s] = 0;
   }
 }
 
@@ -94,10 +97,10 @@ __global__ void SegLenAllKernel(const int* __restrict__ seg_start, const int* __
 // Depth 0: one segment of all `count` active supernodes (only position 0
 // carries a head flag). Writes what the scans and SegStarts / SegLenAll
 // would: every item's inclusive head count is 1, and segment 0's start,
-// length, unfinished flag and item count with both exclusive offsets 0.
+// length and unfinished flag, with both exclusive offsets 0.
 __global__ void DepthZeroKernel(int count, int max_group, int* __restrict__ incl, int* __restrict__ seg_start,
-                                int* __restrict__ seg_len, int* __restrict__ unf_flag, int* __restrict__ unf_len,
-                                int* __restrict__ unf_idx, int* __restrict__ unf_off) {
+                                int* __restrict__ seg_len, int* __restrict__ unf_flag,
+                                unsigned long long* __restrict__ unf_ex) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= count) return;
   incl[p] = 1;
@@ -106,25 +109,23 @@ __global__ void DepthZeroKernel(int count, int max_group, int* __restrict__ incl
     seg_start[0] = 0;
     seg_len[0] = count;
     unf_flag[0] = unf;
-    unf_len[0] = unf ? count : 0;
-    unf_idx[0] = 0;
-    unf_off[0] = 0;
+    unf_ex[0] = 0;
   }
 }
 
-__global__ void DepthCountsKernel(const int* __restrict__ incl_last, const int* __restrict__ unf_idx_last,
-                                  const int* __restrict__ unf_flag_last, const int* __restrict__ unf_off_last,
-                                  const int* __restrict__ unf_len_last, int* __restrict__ out) {
+__global__ void DepthCountsKernel(const int* __restrict__ incl_last, const unsigned long long* __restrict__ ex_last,
+                                  const unsigned long long* __restrict__ pk_last, int* __restrict__ out) {
+  const unsigned long long total = *ex_last + *pk_last;
   out[0] = *incl_last;
-  out[1] = *unf_idx_last + *unf_flag_last;
-  out[2] = *unf_off_last + *unf_len_last;
+  out[1] = static_cast<int>(total >> 32);
+  out[2] = static_cast<int>(total & 0xffffffffull);
 }
 
 // Compact the items of unfinished segments: pos_map[k] = position,
 // item_seg[k] = compact segment index; segment begin/end in compact space.
 __global__ void CompactItemsKernel(const int* __restrict__ incl, const int* __restrict__ seg_start,
                                    const int* __restrict__ seg_len, const int* __restrict__ unf_flag,
-                                   const int* __restrict__ unf_idx, const int* __restrict__ unf_off, int count,
+                                   const unsigned long long* __restrict__ unf_ex, int count,
                                    int* __restrict__ pos_map, int* __restrict__ item_seg,
                                    int* __restrict__ ubeg, int* __restrict__ uend) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -132,12 +133,14 @@ __global__ void CompactItemsKernel(const int* __restrict__ incl, const int* __re
   const int s = incl[p] - 1;
   if (!unf_flag[s]) return;
   const int r = p - seg_start[s];
-  const int k = unf_off[s] + r;
+  const int ui = static_cast<int>(unf_ex[s] >> 32);          // unfinished-segment index
+  const int uo = static_cast<int>(unf_ex[s] & 0xffffffffull);  // its first compact item
+  const int k = uo + r;
   pos_map[k] = p;
-  item_seg[k] = unf_idx[s];
+  item_seg[k] = ui;
   if (r == 0) {
-    ubeg[unf_idx[s]] = unf_off[s];
-    uend[unf_idx[s]] = unf_off[s] + seg_len[s];
+    ubeg[ui] = uo;
+    uend[ui] = uo + seg_len[s];
   }
 }
 
@@ -343,22 +346,24 @@ void Engine::Divide(int iter) {
   const int n = n_;
   const int T = 256;
   cudaStream_t s = stream_;
-  // scratch arrays: d_counts_ holds [flags | scan | seg_len | unf_flag | unf_len | unf_idx | unf_off | ubeg | uend]
+  // scratch arrays: d_counts_ holds [flags | scan | seg_len | unf_flag | unf_len | (2 spare) | ubeg | uend]
   d_counts_.ensure(static_cast<size_t>(n) * 9 + 64);  // + 3 depth counts after uend
   int* flags = d_counts_.p;
   int* scan = flags + n;
   int* seg_len = scan + n;
   int* unf_flag = seg_len + n;
   int* unf_len = unf_flag + n;
-  int* unf_idx = unf_len + n;
-  int* unf_off = unf_idx + n;
-  int* ubeg = unf_off + n;
+  int* ubeg = unf_len + 3 * n;
   int* uend = ubeg + n;
   int* seg_start = d_seg_beg_.p;
   int* item_seg = d_seg_end_.p;
   int* fix_cnt = uend + n + 8;  // mixed-run counter (cleared by each second pass)
   d_fix_list_.ensure(static_cast<size_t>(n) + 1);
   d_keys_hi_[0].ensure(static_cast<size_t>(n) + 1);
+  d_unf_pk_[0].ensure(static_cast<size_t>(n) + 1);
+  d_unf_pk_[1].ensure(static_cast<size_t>(n) + 1);
+  unsigned long long* unf_pk = d_unf_pk_[0].p;  // per segment: unfinished flag << 32 | unfinished items
+  unsigned long long* unf_ex = d_unf_pk_[1].p;  // its exclusive scan
   d_keys_hi_[1].ensure(static_cast<size_t>(n) + 1);
   CheckCuda(cudaMemsetAsync(fix_cnt, 0, sizeof(int), s), "memset mixed-run counter");
 
@@ -420,16 +425,19 @@ void Engine::Divide(int iter) {
       if (depth == 0) {
         ++launches_;
         DepthZeroKernel<<<Blocks(count, T), T, 0, s>>>(count, cfg_.divide_max_group, scan, seg_start, seg_len,
-                                                       unf_flag, unf_len, unf_idx, unf_off);
+                                                       unf_flag, unf_ex);
       } else {
         scan_incl(d_head_flag_.p, scan, count);
         ++launches_;
         SegStartsKernel<<<Blocks(count, T), T, 0, s>>>(d_head_flag_.p, scan, count, seg_start);
         ++launches_;
         SegLenAllKernel<<<Blocks(count, T), T, 0, s>>>(seg_start, scan + count - 1, count, cfg_.divide_max_group,
-                                                       seg_len, unf_flag, unf_len);
-        scan_excl(unf_flag, unf_idx, count);
-        scan_excl(unf_len, unf_off, count);
+                                                       seg_len, unf_flag, unf_pk);
+        size_t pk_bytes = 0;
+        CheckCuda(cub::DeviceScan::ExclusiveSum(nullptr, pk_bytes, unf_pk, unf_ex, count, s), "cub scan size");
+        d_cub_tmp_.ensure(pk_bytes);
+        CheckCuda(cub::DeviceScan::ExclusiveSum(d_cub_tmp_.p, pk_bytes, unf_pk, unf_ex, count, s),
+                  "cub exclusive scan");
       }
       // segments, unfinished segments and their items: known on the host at
       // depth 0 (one segment of all active supernodes), one read-back later
@@ -441,8 +449,7 @@ void Engine::Divide(int iter) {
       } else {
         int* dc = uend + n;
         ++launches_;
-        DepthCountsKernel<<<1, 1, 0, s>>>(scan + count - 1, unf_idx + count - 1, unf_flag + count - 1,
-                                          unf_off + count - 1, unf_len + count - 1, dc);
+        DepthCountsKernel<<<1, 1, 0, s>>>(scan + count - 1, unf_ex + count - 1, unf_pk + count - 1, dc);
         CheckCuda(cudaMemcpyAsync(h_pin_.p, dc, 3 * sizeof(int), cudaMemcpyDeviceToHost, s), "d2h depth counts");
         CheckCuda(cudaStreamSynchronize(s), "sync");
         std::memcpy(hc, h_pin_.p, sizeof(hc));
@@ -455,7 +462,7 @@ void Engine::Divide(int iter) {
       }
       const int items = hc[2];
       ++launches_;
-      CompactItemsKernel<<<Blocks(count, T), T, 0, s>>>(scan, seg_start, seg_len, unf_flag, unf_idx, unf_off, count,
+      CompactItemsKernel<<<Blocks(count, T), T, 0, s>>>(scan, seg_start, seg_len, unf_flag, unf_ex, count,
                                                         d_pos_map_.p, item_seg, ubeg, uend);
       if (fallback) {
         hstats_.divide_fallback_splits += static_cast<uint64_t>(nu);

@@ -280,6 +280,7 @@ class Engine {
   DevBuf<int> d_perm_, d_perm_alt_, d_segkey_, d_segkey_alt_;
   DevBuf<int> d_fix_list_;  // Divide: starts of equal-high-word runs with mixed low words
   DevBuf<unsigned> d_keys_hi_[2];  // Divide: high key words, the radix sort's keys
+  DevBuf<unsigned long long> d_unf_pk_[2];  // Divide: packed unfinished-segment counts and their scan
   DevBuf<int> d_gstart_, d_glen_, d_group_of_, d_idx_in_group_;
   DevBuf<int> d_counts_;
   DevBuf<unsigned char> d_cub_tmp_;

@@ -298,7 +298,8 @@ def run_ours(args, dist: Dist) -> dict | None:
     dominant = args.timed_kernel or "score"
     dist.barrier()
     e.synchronize()
-    clock_log = ROOT / "gpurun_out" / "bench_clocks.csv" if (ROOT / "gpurun_out").exists() else None
+    # the raw nvidia-smi samples of the timed region, when a path is given
+    clock_log = Path(os.environ["BEAM_BENCH_CLOCKS_CSV"]) if os.environ.get("BEAM_BENCH_CLOCKS_CSV") else None
     wall0 = time.perf_counter()
     with ClockSampler(device, clock_log) as clocks:
         t = timed_steps(e, args.steps, dominant)
