@@ -42,7 +42,11 @@ constexpr int kSmemHeads = 4096;     // bucket hash heads in shared memory
 constexpr int kSmemMaxGroup = 48;
 constexpr int kScoreThreads = 256;
 constexpr int kFewGroups = 256;  // blocks of at most this many groups take fewer, wider launches
-constexpr int kSelectMidGroup = 32;   // groups of 9..32 members: a small CTA each
+// Selection by group size: at most kSelectSmallGroup members, a warp each;
+// up to kSelectMidGroup, a small CTA each (sort + greedy pass); larger groups,
+// matching rounds. The two are equal: the matching rounds measured faster
+// than the small CTAs for groups of 9..32 members.
+constexpr int kSelectMidGroup = 8;
 constexpr int kSelectMidThreads = 128;
 constexpr int kSelectMidKeys = 512;   // >= min(C(32,2), 16 * 32) candidates
 constexpr int kRowsThreads = 256;
@@ -1323,7 +1327,7 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareOutputKernel(PrepareParam
 constexpr int kSmallGroup = 32;
 constexpr int kSmallWarps = 4;
 constexpr int kSmallPairs = kSmallGroup * (kSmallGroup - 1) / 2;
-constexpr int kSmallStage = 480;  // staged row entries per group
+constexpr int kSmallStage = 256;  // staged row entries per group
 
 struct SmallWarpSmem {
   long long p[kSmallPairs];  // upper triangle, TriIndex(a, b)
@@ -3519,7 +3523,7 @@ void Engine::RunBlock(const BlockPlan& bp, double threshold, int iter, int total
     // written by this block's prepare kernels
     SP.rc = RowConsts{d_rc_before_.p, d_rc_light_.p, d_rc_heavy_.p, d_rc_nheavy_.p};
   }
-  const int sgrid = static_cast<int>(std::min<long long>((slots + 7) / 8, 152 * 16));
+  const int sgrid = static_cast<int>(std::min<long long>((slots + 7) / 8, 152 * 32));
   // learned ranker: trained after the logging iterations; afterwards the
   // exploration subset is scored first, then the rest above the cutoff
   const bool ranking = cfg_.ranker && rk_trained_ && iter > cfg_.ranker_train_iters;
