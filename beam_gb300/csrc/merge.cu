@@ -1,17 +1,25 @@
 // Merge on the GPU: the blocked EA merge loop (Sweg::Merge, blocked mode,
-// src/sweg.cpp:953-1145) for one 64-group block at a time.
+// src/sweg.cpp:953-1145), one block of group_batch_size groups at a time
+// (64 in the reference's recommended mode; one block of all groups in the
+// batched form).
 //
-//   PrepareKernel   EA-proxy candidates per group (src/sweg.cpp:1598-1727,1800-1999)
-//   ScoreKernel     exact merge gain per candidate pair
-//                   (QuotientGraph::ExactMergeGainPersistentImpl, src/quotient_graph.cpp:340-462)
-//   SelectKernel    reciprocal threshold filter + g0 greedy selection
-//                   (src/sweg.cpp:2146-2186, 2188-2281)
-//   CommitKernel    CommitSelectedPairs + Update_S + QuotientGraph::Merge for
-//                   the block (src/sweg.cpp:2665-2769, 2977-3015,
-//                   src/quotient_graph.cpp:628-742): sizes, internal counts,
-//                   member lists, keep rows rebuilt from keep+remove, neighbour
-//                   rows of removed supernodes rewritten in place
-//   VerifyKernel    optional commit-time re-scoring (--verify-cuda-gain)
+//   Plan*Kernel        the block bookkeeping of a one-block iteration on the
+//                      device (lists and offsets of the groups)
+//   Prepare*Kernel     EA-proxy candidates per group (src/sweg.cpp:1598-1727,
+//                      1800-1999): a warp per small group; big groups by CTA
+//                      or by a GPU-wide sort of their row entries
+//   ScoreKernel        exact merge gain per candidate pair
+//                      (QuotientGraph::ExactMergeGainPersistentImpl,
+//                      src/quotient_graph.cpp:340-462)
+//   Select*Kernel      reciprocal threshold filter + g0 greedy selection
+//                      (src/sweg.cpp:2146-2186, 2188-2281)
+//   Commit*Kernel,     CommitSelectedPairs + Update_S + QuotientGraph::Merge
+//   RewriteRowsKernel  for the block (src/sweg.cpp:2665-2769, 2977-3015,
+//                      src/quotient_graph.cpp:628-742): sizes, internal
+//                      counts, member lists, keep rows rebuilt from
+//                      keep+remove, neighbour rows of removed supernodes
+//                      rewritten in place
+//   VerifyKernel       optional commit-time re-scoring (--verify-cuda-gain)
 //
 // The reference validates every selected pair of a block before applying any
 // of them (Update_S runs after the validation loop), and the pairs of a block
@@ -385,14 +393,15 @@ __device__ void WarpExactGainShared(const QuotientView& Q, const RowConsts& RC, 
 // sel_off, sel_cnt) are indexed by the group's position in the iteration's
 // list of groups with at least two members ("real" groups); real[ri] is the
 // Divide group id. A block covers the real groups [rg0, rg0 + nrg).
-// A big group whose row entries (counted at Divide time, an upper bound for
-// the rest of the iteration: rows of supernodes not yet merged only shrink)
-// exceed the shared-memory bucket table is deferred. PrepareKernel stages its
-// row offsets and member scalars in block scratch; PrepareFillKernel writes
-// one (group, target) key and one (member, count) value per row entry into
-// the group's sort slots, a radix sort brings the entries of every
-// (group, target) together, and PrepareAccumKernel accumulates the member
-// pairs of each run with contiguous reads. No group is bound to one SM.
+// A big group with more than kSmemMaxGroup members, or whose row entries
+// (counted at Divide time, an upper bound for the rest of the iteration: rows
+// of supernodes not yet merged only shrink) exceed the shared-memory bucket
+// table, is deferred. PrepareKernel stages its row offsets and member scalars
+// in block scratch; PrepareFillKernel writes one (group, target) key and one
+// (member, count) value per row entry into the group's sort slots, a radix
+// sort brings the entries of every (group, target) together, and
+// PrepareAccumKernel pairs the entries of each run, a warp per 32 sorted
+// slots. No group is bound to one SM.
 // Scratch layout: eoff int32[g+1] | mq int32[g] | msz int32[g].
 struct BigDesc {
   unsigned char* base;  // nullptr: not deferred
@@ -2819,8 +2828,8 @@ void Engine::ConfigureKernels() {
 
 // Per-iteration layout: the groups with >= 2 members in Divide order, their
 // candidate / selection capacities (min(C(g,2), g*top_k) and g/2) as prefix
-// offsets, pair-table offsets restarting at every 64-group block, and for
-// every block the range of its real groups (empty blocks do no work).
+// offsets, pair-table offsets restarting at every block, and for every block
+// the range of its real groups (empty blocks do no work).
 namespace {
 
 // ---- the plan of a one-block iteration, on the device ----
