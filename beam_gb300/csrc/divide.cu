@@ -7,10 +7,11 @@
 // divide_max_group. The same order is produced breadth-first: every
 // unfinished segment (a run longer than divide_max_group) is already sorted by
 // rep (it is a run of equal hashes of the previous depth, tie-broken by rep),
-// so one stable sort by (segment, next hash) per depth - two stable LSD radix
-// passes over the unfinished items, by hash then by segment index - yields
-// (hash, rep) order inside each segment; equal-hash boundaries become new
-// segment heads. After divide_hash_dims depths the remaining long segments are
+// so one stable sort by (segment, next hash) per depth - stable LSD radix
+// sorts over the unfinished items, by the hash's high word then by segment
+// index, followed by a fix-up that puts runs of equal high words into full
+// hash order - yields (hash, rep) order inside each segment; equal-hash
+// boundaries become new segment heads. After divide_hash_dims depths the remaining long segments are
 // stably sorted by FallbackRank and cut into divide_max_group chunks. Groups
 // are the final segments in position order, exactly the reference's DFS order.
 //
