@@ -1,7 +1,7 @@
 // `beam` command line for the GB300 merge loop. Flags, banner lines and
 // metric.k=v output follow the reference CLI (src/main.cpp:14-110, 327-423,
 // 489-740); the mags-compatible / --scoring-backend cuda guard of
-// src/main.cpp:436-440 is lifted because this build is that backend. Modes
+// src/main.cpp:436-440 is lifted because this library is that backend. Modes
 // outside the recommended one are rejected with an error, as the reference
 // rejects unsupported combinations.
 
@@ -112,7 +112,7 @@ Options ParseArgs(int argc, char** argv) {
     else if (a == "--ea-use-threshold") o.ea_use_threshold = true;
     else if (a == "--write-output") o.write_output = true;
     else if (a == "--verify-cuda-gain") o.verify_cuda_gain = true;  // re-score and check every commit
-    else if (a == "--ranker") o.ranker = true;  // learned candidate ranker (this build's own)
+    else if (a == "--ranker") o.ranker = true;  // learned candidate ranker (beam-gb300's own)
     else if (a == "--ranker-audit") o.ranker_audit = true;
     else if (a == "--ranker-recall" && has) o.ranker_recall = std::stod(take());
     else if (a == "--ranker-train-iters" && has) o.ranker_train_iters = std::stoi(take());

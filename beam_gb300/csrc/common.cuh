@@ -47,8 +47,8 @@ enum Stat : int {
   kStRejNonpositive,          // rejected_nonpositive
   kStTouched,                 // update_touched_quotient_entries
   kStIsolatedGain,            // isolated_gain_sum
-  kStRowsRewritten,           // neighbour rows rewritten (this build's own counter)
-  kStRowEntriesRewritten,     // entries read by row rewrites (this build's own counter)
+  kStRowsRewritten,           // neighbour rows rewritten (beam-gb300's own counter)
+  kStRowEntriesRewritten,     // entries read by row rewrites (beam-gb300's own counter)
   kStDivideMaxGroup,          // divide_max_group_size (atomicMax)
   kStDivideFallback,          // divide_fallback_splits
   kStScoreBytes,              // algorithmic bytes of the scoring kernel
