@@ -12,8 +12,16 @@
 // and the only floating-point operations are IEEE-exact +, -, *, /, floor,
 // frexp and ldexp (this file must be compiled with -ffp-contract=off), so the
 // same seed yields the same edge list on x86-64 and aarch64.
+//
+// Large graphs are built on all host cores with the same result as one
+// thread: R-MAT draws are split into fixed-size chunks whose stream positions
+// are reached by jumping the xoshiro256 state (its update is linear over
+// GF(2), so a jump of k draws is the k-th power of a 256x256 bit matrix), the
+// edge keys are sorted by a stable parallel radix sort, and the CSR rows are
+// filled in parallel and then sorted.
 
 #include <algorithm>
+#include <atomic>
 #include <cerrno>
 #include <cmath>
 #include <cstdint>
@@ -26,6 +34,7 @@
 #include <sstream>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "beam_gb300.h"
@@ -33,6 +42,31 @@
 namespace {
 
 thread_local std::string g_graph_error;
+
+int HostThreads() {
+  const unsigned hc = std::thread::hardware_concurrency();
+  return static_cast<int>(std::max(1u, std::min(hc, 64u)));
+}
+
+// Runs body(t) for t in [0, threads) on that many threads (t == 0 on the caller's).
+template <typename F>
+void ParallelRun(int threads, F&& body) {
+  if (threads <= 1) {
+    body(0);
+    return;
+  }
+  std::vector<std::thread> pool;
+  pool.reserve(static_cast<size_t>(threads - 1));
+  for (int t = 1; t < threads; ++t) pool.emplace_back([&body, t] { body(t); });
+  body(0);
+  for (auto& th : pool) th.join();
+}
+
+// [begin, end) of part t when `count` items are split into `parts` contiguous parts.
+inline int64_t PartBegin(int64_t count, int parts, int t) {
+  return static_cast<int64_t>((static_cast<unsigned __int128>(count) * static_cast<unsigned>(t)) /
+                              static_cast<unsigned>(parts));
+}
 
 struct Rng {
   uint64_t s[4];
@@ -47,8 +81,8 @@ struct Rng {
     for (auto& v : s) v = SplitMix(x);
   }
   static uint64_t Rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
-  uint64_t Next() {
-    const uint64_t result = Rotl(s[1] * 5, 7) * 9;
+  // The state update alone (linear over GF(2)).
+  static void Step(uint64_t* s) {
     const uint64_t t = s[1] << 17;
     s[2] ^= s[0];
     s[3] ^= s[1];
@@ -56,6 +90,10 @@ struct Rng {
     s[0] ^= s[3];
     s[2] ^= t;
     s[3] = Rotl(s[3], 45);
+  }
+  uint64_t Next() {
+    const uint64_t result = Rotl(s[1] * 5, 7) * 9;
+    Step(s);
     return result;
   }
   // 53-bit uniform integer; compare with Threshold(p) for a Bernoulli draw.
@@ -66,10 +104,148 @@ struct Rng {
   }
 };
 
+// 256x256 matrix over GF(2) acting on the xoshiro256 state: bit i of the
+// state is bit (i % 64) of word i / 64; row i holds the coefficients of
+// output bit i.
+struct StateMatrix {
+  uint64_t row[256][4];
+
+  static StateMatrix Identity() {
+    StateMatrix m{};
+    for (int i = 0; i < 256; ++i) m.row[i][i / 64] = uint64_t{1} << (i % 64);
+    return m;
+  }
+  // The matrix of one Rng::Step: column j is the step applied to unit state j.
+  static StateMatrix OneStep() {
+    StateMatrix m{};
+    for (int j = 0; j < 256; ++j) {
+      uint64_t s[4] = {0, 0, 0, 0};
+      s[j / 64] = uint64_t{1} << (j % 64);
+      Rng::Step(s);
+      for (int i = 0; i < 256; ++i) {
+        if ((s[i / 64] >> (i % 64)) & 1) m.row[i][j / 64] |= uint64_t{1} << (j % 64);
+      }
+    }
+    return m;
+  }
+  StateMatrix operator*(const StateMatrix& b) const {
+    StateMatrix c{};
+    for (int i = 0; i < 256; ++i) {
+      for (int k = 0; k < 256; ++k) {
+        if ((row[i][k / 64] >> (k % 64)) & 1) {
+          for (int w = 0; w < 4; ++w) c.row[i][w] ^= b.row[k][w];
+        }
+      }
+    }
+    return c;
+  }
+  void Apply(const uint64_t* x, uint64_t* y) const {
+    uint64_t out[4] = {0, 0, 0, 0};
+    for (int i = 0; i < 256; ++i) {
+      const uint64_t dot = (row[i][0] & x[0]) ^ (row[i][1] & x[1]) ^ (row[i][2] & x[2]) ^ (row[i][3] & x[3]);
+      out[i / 64] |= static_cast<uint64_t>(__builtin_parityll(dot)) << (i % 64);
+    }
+    std::memcpy(y, out, sizeof(out));
+  }
+  // The matrix that advances a stream by `steps` draws.
+  static StateMatrix Jump(uint64_t steps) {
+    StateMatrix result = Identity();
+    StateMatrix base = OneStep();
+    while (steps) {
+      if (steps & 1) result = result * base;
+      steps >>= 1;
+      if (steps) base = base * base;
+    }
+    return result;
+  }
+};
+
 uint64_t Threshold(double p) {
   if (!(p > 0.0)) return 0;
   if (p >= 1.0) return uint64_t{1} << 53;
   return static_cast<uint64_t>(p * 0x1.0p53);
+}
+
+// Stable LSD radix sort of the low `bits` bits of every key, on all cores.
+void ParallelRadixSort(std::vector<uint64_t>& keys, int bits) {
+  const int64_t count = static_cast<int64_t>(keys.size());
+  if (count < (1 << 16)) {
+    std::stable_sort(keys.begin(), keys.end(), [bits](uint64_t a, uint64_t b) {
+      const uint64_t mask = bits >= 64 ? ~uint64_t{0} : ((uint64_t{1} << bits) - 1);
+      return (a & mask) < (b & mask);
+    });
+    return;
+  }
+  const int passes = std::max(1, (bits + 11) / 12);
+  const int width = (bits + passes - 1) / passes;
+  const size_t buckets = size_t{1} << width;
+  const int threads = HostThreads();
+  std::vector<uint64_t> tmp(keys.size());
+  std::vector<int64_t> hist(static_cast<size_t>(threads) * buckets);
+  uint64_t* src = keys.data();
+  uint64_t* dst = tmp.data();
+  for (int p = 0; p < passes; ++p) {
+    const int shift = p * width;
+    const uint64_t mask = buckets - 1;
+    std::fill(hist.begin(), hist.end(), 0);
+    ParallelRun(threads, [&](int t) {
+      int64_t* h = hist.data() + static_cast<size_t>(t) * buckets;
+      for (int64_t i = PartBegin(count, threads, t), e = PartBegin(count, threads, t + 1); i < e; ++i) {
+        ++h[(src[i] >> shift) & mask];
+      }
+    });
+    // exclusive offsets in (digit, part) order keep the sort stable
+    int64_t acc = 0;
+    for (size_t d = 0; d < buckets; ++d) {
+      for (int t = 0; t < threads; ++t) {
+        int64_t& h = hist[static_cast<size_t>(t) * buckets + d];
+        const int64_t c = h;
+        h = acc;
+        acc += c;
+      }
+    }
+    ParallelRun(threads, [&](int t) {
+      int64_t* h = hist.data() + static_cast<size_t>(t) * buckets;
+      for (int64_t i = PartBegin(count, threads, t), e = PartBegin(count, threads, t + 1); i < e; ++i) {
+        dst[h[(src[i] >> shift) & mask]++] = src[i];
+      }
+    });
+    std::swap(src, dst);
+  }
+  if (src != keys.data()) keys.swap(tmp);
+}
+
+// Sorted, duplicate-free copy of the packed (lo << 32 | hi) edge keys, where
+// every id is below 2^id_bits.
+void SortUniqueEdges(std::vector<uint64_t>& packed, int id_bits) {
+  const int64_t count = static_cast<int64_t>(packed.size());
+  const int threads = HostThreads();
+  // (lo << 32 | hi) -> (lo << id_bits | hi): the sort covers 2 * id_bits bits
+  ParallelRun(threads, [&](int t) {
+    for (int64_t i = PartBegin(count, threads, t), e = PartBegin(count, threads, t + 1); i < e; ++i) {
+      packed[i] = ((packed[i] >> 32) << id_bits) | (packed[i] & 0xffffffffu);
+    }
+  });
+  ParallelRadixSort(packed, 2 * id_bits);
+  // keep the first key of each run of equal keys, restoring the (lo << 32 | hi) form
+  std::vector<int64_t> kept(static_cast<size_t>(threads) + 1, 0);
+  ParallelRun(threads, [&](int t) {
+    int64_t c = 0;
+    for (int64_t i = PartBegin(count, threads, t), e = PartBegin(count, threads, t + 1); i < e; ++i) {
+      c += (i == 0 || packed[i] != packed[i - 1]) ? 1 : 0;
+    }
+    kept[static_cast<size_t>(t) + 1] = c;
+  });
+  for (int t = 0; t < threads; ++t) kept[static_cast<size_t>(t) + 1] += kept[static_cast<size_t>(t)];
+  std::vector<uint64_t> out(static_cast<size_t>(kept[static_cast<size_t>(threads)]));
+  const uint64_t low = (uint64_t{1} << id_bits) - 1;
+  ParallelRun(threads, [&](int t) {
+    int64_t o = kept[static_cast<size_t>(t)];
+    for (int64_t i = PartBegin(count, threads, t), e = PartBegin(count, threads, t + 1); i < e; ++i) {
+      if (i == 0 || packed[i] != packed[i - 1]) out[o++] = ((packed[i] >> id_bits) << 32) | (packed[i] & low);
+    }
+  });
+  packed.swap(out);
 }
 
 // Deterministic natural log / exp built from IEEE-exact basic operations only.
@@ -114,19 +290,24 @@ struct EdgeList {
 // original-id order; otherwise ids are kept and n = max id + 1, as the text
 // loader computes it, so isolated ids below the maximum stay as nodes.
 EdgeList CanonicalEdges(std::vector<uint64_t>& packed, bool relabel) {
-  std::sort(packed.begin(), packed.end());
-  packed.erase(std::unique(packed.begin(), packed.end()), packed.end());
+  uint64_t max_hi = 0;
+  for (uint64_t key : packed) max_hi = std::max<uint64_t>(max_hi, key & 0xffffffffu);
+  int id_bits = 1;
+  while (id_bits < 32 && (max_hi >> id_bits) != 0) ++id_bits;
+  SortUniqueEdges(packed, id_bits);
   if (!relabel) {
     EdgeList out;
+    const int64_t count = static_cast<int64_t>(packed.size());
     out.u.resize(packed.size());
     out.v.resize(packed.size());
-    int64_t max_id = -1;
-    for (size_t i = 0; i < packed.size(); ++i) {
-      out.u[i] = static_cast<int32_t>(packed[i] >> 32);
-      out.v[i] = static_cast<int32_t>(packed[i] & 0xffffffffu);
-      max_id = std::max<int64_t>(max_id, out.v[i]);
-    }
-    out.n = max_id + 1;
+    const int threads = HostThreads();
+    ParallelRun(threads, [&](int t) {
+      for (int64_t i = PartBegin(count, threads, t), e = PartBegin(count, threads, t + 1); i < e; ++i) {
+        out.u[i] = static_cast<int32_t>(packed[i] >> 32);
+        out.v[i] = static_cast<int32_t>(packed[i] & 0xffffffffu);
+      }
+    });
+    out.n = packed.empty() ? 0 : static_cast<int64_t>(max_hi) + 1;
     return out;
   }
   std::vector<uint32_t> ids;
@@ -157,28 +338,71 @@ inline void PushEdge(std::vector<uint64_t>& packed, uint64_t a, uint64_t b) {
 }
 
 // R-MAT: each edge picks one of four quadrants per level with probabilities
-// (a, b, c, d).
+// (a, b, c, d), one draw of the seed's stream per level, edges in order.
+// Chunks of kRmatChunk edges run in parallel from jumped stream positions;
+// the key list is the one a single pass over the stream produces.
 void GenRmat(std::vector<uint64_t>& packed, int scale, double edge_factor, double a, double b,
              double c, uint64_t seed) {
   if (scale < 1 || scale > 30) throw std::invalid_argument("rmat scale must be in [1, 30]");
-  Rng rng(seed);
+  constexpr int64_t kRmatChunk = int64_t{1} << 16;
   const uint64_t ta = Threshold(a);
   const uint64_t tb = Threshold(a + b);
   const uint64_t tc = Threshold(a + b + c);
   const int64_t samples = static_cast<int64_t>(edge_factor * static_cast<double>(int64_t{1} << scale));
-  packed.reserve(packed.size() + static_cast<size_t>(samples));
-  for (int64_t e = 0; e < samples; ++e) {
-    uint64_t row = 0;
-    uint64_t col = 0;
-    for (int level = 0; level < scale; ++level) {
-      const uint64_t r = rng.Next53();
-      const uint64_t bit_row = r >= tb ? 1 : 0;
-      const uint64_t bit_col = (r >= ta && r < tb) || r >= tc ? 1 : 0;
-      row = (row << 1) | bit_row;
-      col = (col << 1) | bit_col;
+  if (samples <= 0) return;
+  const int64_t chunks = (samples + kRmatChunk - 1) / kRmatChunk;
+  // stream state at the start of every chunk
+  std::vector<uint64_t> starts(static_cast<size_t>(chunks) * 4);
+  {
+    Rng rng(seed);
+    const StateMatrix jump = StateMatrix::Jump(static_cast<uint64_t>(kRmatChunk) * static_cast<uint64_t>(scale));
+    uint64_t s[4] = {rng.s[0], rng.s[1], rng.s[2], rng.s[3]};
+    for (int64_t ch = 0; ch < chunks; ++ch) {
+      std::memcpy(&starts[static_cast<size_t>(ch) * 4], s, sizeof(s));
+      if (ch + 1 < chunks) jump.Apply(s, s);
     }
-    PushEdge(packed, row, col);
   }
+  constexpr uint64_t kLoop = ~uint64_t{0};
+  std::vector<uint64_t> keys(static_cast<size_t>(samples));
+  const int threads = HostThreads();
+  std::atomic<int64_t> next_chunk{0};
+  ParallelRun(threads, [&](int) {
+    for (int64_t ch = next_chunk++; ch < chunks; ch = next_chunk++) {
+      Rng rng(0);
+      std::memcpy(rng.s, &starts[static_cast<size_t>(ch) * 4], sizeof(rng.s));
+      const int64_t e1 = std::min(samples, (ch + 1) * kRmatChunk);
+      for (int64_t e = ch * kRmatChunk; e < e1; ++e) {
+        uint64_t row = 0;
+        uint64_t col = 0;
+        for (int level = 0; level < scale; ++level) {
+          const uint64_t r = rng.Next53();
+          const uint64_t bit_row = r >= tb ? 1 : 0;
+          const uint64_t bit_col = (r >= ta && r < tb) || r >= tc ? 1 : 0;
+          row = (row << 1) | bit_row;
+          col = (col << 1) | bit_col;
+        }
+        keys[static_cast<size_t>(e)] = row == col ? kLoop : (std::min(row, col) << 32) | std::max(row, col);
+      }
+    }
+  });
+  // drop the self-loops, keeping the draw order
+  std::vector<int64_t> kept(static_cast<size_t>(threads) + 1, 0);
+  ParallelRun(threads, [&](int t) {
+    int64_t cnt = 0;
+    for (int64_t i = PartBegin(samples, threads, t), e = PartBegin(samples, threads, t + 1); i < e; ++i) {
+      cnt += keys[static_cast<size_t>(i)] != kLoop ? 1 : 0;
+    }
+    kept[static_cast<size_t>(t) + 1] = cnt;
+  });
+  for (int t = 0; t < threads; ++t) kept[static_cast<size_t>(t) + 1] += kept[static_cast<size_t>(t)];
+  const size_t base = packed.size();
+  packed.resize(base + static_cast<size_t>(kept[static_cast<size_t>(threads)]));
+  ParallelRun(threads, [&](int t) {
+    size_t o = base + static_cast<size_t>(kept[static_cast<size_t>(t)]);
+    for (int64_t i = PartBegin(samples, threads, t), e = PartBegin(samples, threads, t + 1); i < e; ++i) {
+      if (keys[static_cast<size_t>(i)] != kLoop) packed[o++] = keys[static_cast<size_t>(i)];
+    }
+  });
 }
 
 // Power-law weights w_i = (i + i0)^(-1/(gamma-1)), i = 0..n-1.
@@ -411,24 +635,109 @@ struct beam_graph {
 namespace {
 
 // Symmetric CSR with sorted neighbour lists (reference loader semantics).
+// first[x] = first position i with key(i) >= x, for x in [0, n], over a
+// list of `count` non-decreasing keys.
+template <typename Key>
+void RunStarts(int64_t count, int64_t n, Key key, int64_t* first, int threads) {
+  ParallelRun(threads, [&](int t) {
+    for (int64_t i = PartBegin(count, threads, t), e = PartBegin(count, threads, t + 1); i < e; ++i) {
+      const int64_t lo = i == 0 ? 0 : key(i - 1) + 1;
+      for (int64_t x = lo, hi = key(i); x <= hi; ++x) first[x] = i;
+    }
+  });
+  for (int64_t x = count == 0 ? 0 : key(count - 1) + 1; x <= n; ++x) first[x] = count;
+}
+
+// CSR of a strictly increasing (u, v) edge list with u < v (the generators'
+// output): row x is the u of every edge (u, x), ascending, then the v of every
+// edge (x, v), ascending, with no per-row sort. The (v, u) order of the first
+// part comes from a stable radix sort by v.
+bool BuildCsrSorted(beam_graph* g, int threads) {
+  const int64_t n = g->n;
+  const int64_t edges = static_cast<int64_t>(g->eu.size());
+  const int32_t* eu = g->eu.data();
+  const int32_t* ev = g->ev.data();
+  std::atomic<bool> sorted{true};
+  ParallelRun(threads, [&](int t) {
+    for (int64_t i = PartBegin(edges, threads, t), e = PartBegin(edges, threads, t + 1); i < e; ++i) {
+      if (eu[i] >= ev[i] || ev[i] >= n || eu[i] < 0 ||
+          (i > 0 && (eu[i - 1] > eu[i] || (eu[i - 1] == eu[i] && ev[i - 1] >= ev[i])))) {
+        sorted = false;
+        break;
+      }
+    }
+  });
+  if (!sorted) return false;
+  int id_bits = 1;
+  while (id_bits < 32 && ((n - 1) >> id_bits) != 0) ++id_bits;
+  std::vector<uint64_t> tr(static_cast<size_t>(edges));
+  ParallelRun(threads, [&](int t) {
+    for (int64_t i = PartBegin(edges, threads, t), e = PartBegin(edges, threads, t + 1); i < e; ++i) {
+      tr[i] = (static_cast<uint64_t>(eu[i]) << 32) | static_cast<uint32_t>(ev[i]);
+    }
+  });
+  ParallelRadixSort(tr, id_bits);  // by v, u ascending within equal v (stable)
+  std::vector<int64_t> fwd(static_cast<size_t>(n) + 1);
+  std::vector<int64_t> bwd(static_cast<size_t>(n) + 1);
+  RunStarts(edges, n, [&](int64_t i) { return static_cast<int64_t>(eu[i]); }, fwd.data(), threads);
+  RunStarts(edges, n, [&](int64_t i) { return static_cast<int64_t>(tr[i] & 0xffffffffu); }, bwd.data(), threads);
+  g->row_ptr.resize(static_cast<size_t>(n) + 1);
+  int64_t* rp = g->row_ptr.data();
+  ParallelRun(threads, [&](int t) {
+    for (int64_t x = PartBegin(n + 1, threads, t), e = PartBegin(n + 1, threads, t + 1); x < e; ++x) {
+      rp[x] = fwd[x] + bwd[x];
+    }
+  });
+  g->col_idx.resize(static_cast<size_t>(2 * edges));
+  int32_t* col = g->col_idx.data();
+  ParallelRun(threads, [&](int t) {
+    for (int64_t x = PartBegin(n, threads, t), e = PartBegin(n, threads, t + 1); x < e; ++x) {
+      int64_t o = rp[x];
+      for (int64_t i = bwd[x]; i < bwd[x + 1]; ++i) col[o++] = static_cast<int32_t>(tr[i] >> 32);
+      for (int64_t i = fwd[x]; i < fwd[x + 1]; ++i) col[o++] = ev[i];
+    }
+  });
+  return true;
+}
+
+// Rows are filled in parallel (arbitrary order within a row) and then sorted;
+// a row's values are equal-or-distinct ids, so the sorted row is the same for
+// any fill order.
 void BuildCsr(beam_graph* g) {
   const int64_t n = g->n;
+  const int64_t edges = static_cast<int64_t>(g->eu.size());
+  const int threads = edges < (1 << 16) ? 1 : HostThreads();
+  if (edges >= (1 << 16) && BuildCsrSorted(g, threads)) return;
   g->row_ptr.assign(static_cast<size_t>(n + 1), 0);
-  for (size_t i = 0; i < g->eu.size(); ++i) {
-    g->row_ptr[static_cast<size_t>(g->eu[i]) + 1]++;
-    g->row_ptr[static_cast<size_t>(g->ev[i]) + 1]++;
-  }
-  for (int64_t i = 0; i < n; ++i) g->row_ptr[static_cast<size_t>(i + 1)] += g->row_ptr[static_cast<size_t>(i)];
-  g->col_idx.assign(static_cast<size_t>(g->row_ptr[static_cast<size_t>(n)]), 0);
+  int64_t* rp = g->row_ptr.data();
+  const int32_t* eu = g->eu.data();
+  const int32_t* ev = g->ev.data();
+  ParallelRun(threads, [&](int t) {
+    for (int64_t i = PartBegin(edges, threads, t), e = PartBegin(edges, threads, t + 1); i < e; ++i) {
+      __atomic_fetch_add(&rp[eu[i] + 1], int64_t{1}, __ATOMIC_RELAXED);
+      __atomic_fetch_add(&rp[ev[i] + 1], int64_t{1}, __ATOMIC_RELAXED);
+    }
+  });
+  for (int64_t i = 0; i < n; ++i) rp[i + 1] += rp[i];
+  g->col_idx.assign(static_cast<size_t>(rp[n]), 0);
+  int32_t* col = g->col_idx.data();
   std::vector<int64_t> cur(g->row_ptr.begin(), g->row_ptr.end() - 1);
-  for (size_t i = 0; i < g->eu.size(); ++i) {
-    g->col_idx[static_cast<size_t>(cur[static_cast<size_t>(g->eu[i])]++)] = g->ev[i];
-    g->col_idx[static_cast<size_t>(cur[static_cast<size_t>(g->ev[i])]++)] = g->eu[i];
-  }
-  for (int64_t v = 0; v < n; ++v) {
-    std::sort(g->col_idx.begin() + g->row_ptr[static_cast<size_t>(v)],
-              g->col_idx.begin() + g->row_ptr[static_cast<size_t>(v + 1)]);
-  }
+  int64_t* cp = cur.data();
+  ParallelRun(threads, [&](int t) {
+    for (int64_t i = PartBegin(edges, threads, t), e = PartBegin(edges, threads, t + 1); i < e; ++i) {
+      col[__atomic_fetch_add(&cp[eu[i]], int64_t{1}, __ATOMIC_RELAXED)] = ev[i];
+      col[__atomic_fetch_add(&cp[ev[i]], int64_t{1}, __ATOMIC_RELAXED)] = eu[i];
+    }
+  });
+  std::atomic<int64_t> next_rows{0};
+  constexpr int64_t kRows = 4096;
+  ParallelRun(threads, [&](int) {
+    for (int64_t r0 = next_rows.fetch_add(kRows); r0 < n; r0 = next_rows.fetch_add(kRows)) {
+      for (int64_t v = r0, r1 = std::min(n, r0 + kRows); v < r1; ++v) {
+        std::sort(col + rp[v], col + rp[v + 1]);
+      }
+    }
+  });
 }
 
 beam_graph* FromEdges(int64_t n, std::vector<int32_t>&& u, std::vector<int32_t>&& v) {

@@ -69,3 +69,19 @@ def test_relabel_option():
     assert r.edges == g.edges and r.n < g.n
     deg = np.diff(r.row_ptr)
     assert (deg > 0).all()
+
+
+def test_sorted_fast_csr_equals_generic_csr():
+    """Generated edge lists take the sorted-list CSR build; the same edges in
+    shuffled order take the generic fill-and-sort build. Both give one CSR."""
+    from beam_gb300 import Graph
+    g = Graph.generate("rmat:scale=15,ef=8,seed=5")
+    assert g.edges >= 1 << 16
+    u, v = g.edge_list()
+    perm = np.random.default_rng(0).permutation(len(u))
+    swap = np.random.default_rng(1).random(len(u)) < 0.5
+    uu = np.where(swap, v, u)[perm]
+    vv = np.where(swap, u, v)[perm]
+    h = Graph.from_edges(uu, vv)
+    assert h.n == g.n
+    assert np.array_equal(h.row_ptr, g.row_ptr) and np.array_equal(h.col_idx, g.col_idx)
