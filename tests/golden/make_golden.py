@@ -2,7 +2,8 @@
 
 The reference (githubofzby/beam) is compiled from its own sources into
 oracle/_ref/beam_ref by `make -C oracle ref` (needs the sources under
-/root/reference, present only where the fixtures are made). Each case is a
+the directory named by BEAM_REFERENCE_DIR, present only where the fixtures
+are made). Each case is a
 graph (a generator spec of beam_gb300's seeded generators, or an explicit
 edge list) plus reference flags; the fixture keeps the reference's metric
 lines that the GB300 path must reproduce, the SHA-256 of its G.txt, P.txt,
@@ -128,6 +129,14 @@ CASES += [
      "large": True},
     {"name": "union_batched", "spec": WORKLOADS["grid_chunglu_union"], "flags": flags_with(group_batch_size=1 << 30),
      "large": True, "huge": True},
+    # the plain form (64-group blocks) of the grid + Chung-Lu union
+    {"name": "union_plain", "spec": WORKLOADS["grid_chunglu_union"], "flags": flags_with(), "large": True,
+     "huge": True},
+    # the 4M-node Chung-Lu graph with 200k planted twin groups, first 5 iterations
+    {"name": "chunglu4m_twins_it5", "spec": WORKLOADS["chunglu4m_twins"], "flags": flags_with(iterations=5),
+     "large": True, "huge": True},
+    # R-MAT scale 24, edge factor 16: the large single-GPU run, plain form
+    {"name": "rmat24", "spec": WORKLOADS["rmat24"], "flags": flags_with(), "large": True, "huge": True},
 ]
 
 
@@ -135,15 +144,17 @@ def edge_text(edges) -> str:
     return "".join(f"{u} {v}\n" for u, v in edges)
 
 
-def graph_checksum(text: str) -> str:
-    return hashlib.sha256(text.encode()).hexdigest()
+def file_checksum(path: Path) -> str:
+    h = hashlib.sha256()
+    with open(path, "rb") as f:
+        for block in iter(lambda: f.read(1 << 24), b""):
+            h.update(block)
+    return h.hexdigest()
 
 
-def run_reference(text: str, flags: list[str], tmp: Path) -> tuple[dict, dict, str]:
-    graph = tmp / "graph.txt"
-    graph.write_text(text)
+def run_reference(graph: Path, flags: list[str], tmp: Path, threads: int) -> tuple[dict, dict, str]:
     out = tmp / "out"
-    env = dict(os.environ, OMP_NUM_THREADS=str(os.cpu_count() or 1))
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
     proc = subprocess.run([str(REF_BIN), "--input", str(graph), *flags, "--write-output", "--out", str(out)],
                           capture_output=True, text=True, env=env)
     metrics = {}
@@ -155,13 +166,14 @@ def run_reference(text: str, flags: list[str], tmp: Path) -> tuple[dict, dict, s
     hashes = {}
     if proc.returncode == 0:
         for f in ("G.txt", "P.txt", "Cp.txt", "Cm.txt"):
-            hashes[f] = hashlib.sha256((out / f).read_bytes()).hexdigest()
+            hashes[f] = file_checksum(out / f)
     return metrics, hashes, proc.stdout + proc.stderr
 
 
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", nargs="*")
+    ap.add_argument("--threads", type=int, default=os.cpu_count() or 1, help="OpenMP threads of the reference")
     args = ap.parse_args()
     if not REF_BIN.exists():
         subprocess.run(["make", "-C", str(ROOT / "oracle"), "ref"], check=True)
@@ -170,14 +182,15 @@ def main() -> None:
     for case in CASES:
         if args.only and case["name"] not in args.only:
             continue
-        if "spec" in case:
-            g = Graph.generate(case["spec"])
-            u, v = g.edge_list()
-            text = edge_text(zip(u.tolist(), v.tolist()))
-        else:
-            text = edge_text(case["edges"])
         with tempfile.TemporaryDirectory() as td:
-            metrics, hashes, log = run_reference(text, case["flags"], Path(td))
+            graph = Path(td) / "graph.txt"
+            if "spec" in case:
+                # the library's writer prints the generated edge list as "u v" lines
+                Graph.generate(case["spec"]).write_text(graph)
+            else:
+                graph.write_text(edge_text(case["edges"]))
+            checksum = file_checksum(graph)
+            metrics, hashes, log = run_reference(graph, case["flags"], Path(td), args.threads)
         if not hashes:
             raise RuntimeError(f"reference failed on {case['name']}:\n{log}")
         entry = {k: case[k] for k in ("name", "flags") }
@@ -187,7 +200,7 @@ def main() -> None:
             entry["edges"] = case["edges"]
         entry["large"] = bool(case.get("large"))
         entry["huge"] = bool(case.get("huge"))  # too slow for the CPU oracle in the CPU suite
-        entry["graph_sha256"] = graph_checksum(text)
+        entry["graph_sha256"] = checksum
         entry["metrics"] = metrics
         entry["files_sha256"] = hashes
         keep[case["name"]] = entry
@@ -195,7 +208,9 @@ def main() -> None:
     errors = []
     for name, (edges, message) in ERROR_CASES.items():
         with tempfile.TemporaryDirectory() as td:
-            metrics, hashes, log = run_reference(edge_text(edges), flags_with(), Path(td))
+            graph = Path(td) / "graph.txt"
+            graph.write_text(edge_text(edges))
+            metrics, hashes, log = run_reference(graph, flags_with(), Path(td), args.threads)
         assert not hashes and message in log, log
         errors.append({"name": name, "edges": edges, "message": message})
     order = [c["name"] for c in CASES]
