@@ -10,9 +10,11 @@
 // cudaMalloc'd scratch.
 //
 // Limits: at most kNoAllocMaxRows members, kNoAllocMaxEntries row entries in
-// total and top_k at most kNoAllocMaxTopK; larger requests are rejected
-// before anything is launched. The array (kNoAllocScratchBytes) is held by
-// every GPU that loads the library until the process exits.
+// total and 1 <= top_k <= kNoAllocMaxTopK; other requests are rejected
+// before anything is launched. Row weights must lie in [0, 2^32) (the kernel
+// stages them as 32-bit words); the kernel's validation pass rejects others.
+// The array (kNoAllocScratchBytes) is held by every GPU that loads the
+// library until the process exits.
 //
 // Semantics are those of the engine's prepare step (PrepareBatchEncodingAware-
 // GroupWithWorkspace, legacy EA-proxy branch, src/sweg.cpp:1800-1999): the
@@ -99,14 +101,21 @@ __global__ void __launch_bounds__(kNoAllocThreads) PrepareFlatKernel(FlatArgs A,
   int* enx = reinterpret_cast<int*>(ee + kNoAllocMaxEntries);
   const unsigned hmask = kNoAllocHeads - 1;
 
+  // s_bad bits: 1 = offsets, 2 = repeated reps, 4 = weight out of range
   if (tid == 0) {
-    s_bad = A.offsets[0] != 0 || static_cast<long long>(A.offsets[g]) != A.entries;
+    s_bad = (A.offsets[0] != 0 || static_cast<long long>(A.offsets[g]) != A.entries) ? 1 : 0;
     *status = 0;
   }
   for (int i = tid; i < g; i += kNoAllocThreads) s_rep[i] = A.reps[i];
   __syncthreads();
   for (int i = tid; i < g; i += kNoAllocThreads) {
-    if (A.offsets[i] > A.offsets[i + 1] || A.offsets[i + 1] > A.entries) s_bad = 1;
+    if (A.offsets[i] > A.offsets[i + 1] || A.offsets[i + 1] > A.entries) atomicOr(&s_bad, 1);
+  }
+  // counts are staged as 32-bit words: a weight outside [0, 2^32) is an error,
+  // never a silently truncated count
+  for (long long k = tid; k < A.entries; k += kNoAllocThreads) {
+    const long long c = A.wt[k];
+    if (c < 0 || c > static_cast<long long>(0xffffffffu)) atomicOr(&s_bad, 4);
   }
   // clear what must start at zero: every call reuses the same array
   for (long long k = tid; k < gg; k += kNoAllocThreads) {
@@ -117,7 +126,7 @@ __global__ void __launch_bounds__(kNoAllocThreads) PrepareFlatKernel(FlatArgs A,
   __syncthreads();
   if (s_bad) {
     if (tid == 0) {
-      *status = 1;
+      *status = (s_bad & 1) ? 1 : 3;
       *A.out_count = -1;
     }
     return;
@@ -131,7 +140,7 @@ __global__ void __launch_bounds__(kNoAllocThreads) PrepareFlatKernel(FlatArgs A,
   }
   __syncthreads();
   for (int i = tid + 1; i < g; i += kNoAllocThreads) {
-    if (s_sorted_rep[i] == s_sorted_rep[i - 1]) s_bad = 1;
+    if (s_sorted_rep[i] == s_sorted_rep[i - 1]) atomicOr(&s_bad, 2);
   }
   __syncthreads();
   if (s_bad) {
@@ -206,9 +215,9 @@ __global__ void __launch_bounds__(kNoAllocThreads) PrepareFlatKernel(FlatArgs A,
     if (j < i) pmat[idx] = pmat[static_cast<long long>(j) * g + i];
   }
   __syncthreads();
-  // per member: positive partners ranked by ratio, the top_k kept
-  int top_k = A.top_k < g - 1 ? A.top_k : g - 1;
-  if (top_k < 1) top_k = 1;
+  // per member: positive partners ranked by ratio, the top_k kept (top_k >= 1
+  // is checked by the host)
+  const int top_k = A.top_k < g - 1 ? A.top_k : g - 1;
   for (int i = warp; i < g; i += nwarps) {
     const long long* prow = pmat + static_cast<long long>(i) * g;
     double* rrow = rmat + static_cast<long long>(i) * g;
@@ -352,8 +361,9 @@ int beam_prepare_flat_noalloc(const int32_t* offsets, const int32_t* row_rep_ids
     return Fail("top_k=" + std::to_string(top_k) + " exceeds the no-allocation limit of " +
                 std::to_string(kNoAllocMaxTopK));
   }
+  if (top_k < 1) return Fail("top_k=" + std::to_string(top_k) + " must be at least 1");
   const long long g = rows;
-  const long long k = top_k > 1 ? top_k : 1;
+  const long long k = top_k;
   const long long need = g >= 2 ? std::min(g * (g - 1) / 2, g * k) : 0;
   if (out_capacity < need) {
     return Fail("out_capacity=" + std::to_string(out_capacity) + " is below min(C(rows,2), rows*top_k)=" +
@@ -365,8 +375,9 @@ int beam_prepare_flat_noalloc(const int32_t* offsets, const int32_t* row_rep_ids
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (rows < 2) {
-    const cudaError_t st = cudaMemsetAsync(out_count, 0, sizeof(int32_t), s);
-    if (st != cudaSuccess) return Fail(std::string("cudaMemsetAsync: ") + cudaGetErrorString(st));
+    cudaError_t st = cudaMemsetAsync(out_count, 0, sizeof(int32_t), s);
+    if (st == cudaSuccess) st = cudaStreamSynchronize(s);
+    if (st != cudaSuccess) return Fail(std::string("cuda: ") + cudaGetErrorString(st));
     return 0;
   }
   int dev = 0;
@@ -398,6 +409,7 @@ int beam_prepare_flat_noalloc(const int32_t* offsets, const int32_t* row_rep_ids
   if (st != cudaSuccess) return Fail(std::string("cuda: ") + cudaGetErrorString(st));
   if (status == 1) return Fail("offsets must rise from 0 to num_entries");
   if (status == 2) return Fail("row_rep_ids must be distinct");
+  if (status == 3) return Fail("weights must lie in [0, 2^32): the kernel stages counts as 32-bit words");
   return 0;
 }
 
