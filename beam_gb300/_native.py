@@ -86,6 +86,14 @@ class Encoding(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class FlatScorerStats(C.Structure):
+    _fields_ = [(name, i64) for name in ("calls", "kernel_launches", "pairs", "h2d_bytes", "d2h_bytes",
+                                          "max_pairs_per_launch")] + [("kernel_ms", f64)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 TIME_NONE, TIME_SCORE, TIME_PREPARE, TIME_UPDATE, TIME_DIVIDE = 0, 1, 2, 3, 4
 
 # name -> (restype, argtypes); every symbol declared in include/beam_gb300.h
@@ -136,6 +144,13 @@ SIGNATURES = {
     "beam_engine_last_error": (C.c_char_p, []),
     "beam_prepare_flat_noalloc": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, i32, i64, i32, vp, vp, i64, vp, vp]),
     "beam_prepare_flat_noalloc_last_error": (C.c_char_p, []),
+    "beam_flat_scorer_create": (C.c_int, [i32, C.POINTER(vp)]),
+    "beam_flat_scorer_destroy": (None, [vp]),
+    "beam_flat_scorer_get_stats": (C.c_int, [vp, C.POINTER(FlatScorerStats)]),
+    "beam_flat_scorer_memory_budget": (C.c_int, [vp, P_i64]),
+    "beam_flat_scorer_score": (C.c_int, [vp, P_i32, i64, P_i32, P_i32, P_i64, P_i64, i32, P_i32, P_i64, P_i64, i64,
+                                         P_i64, P_i64]),
+    "beam_flat_scorer_last_error": (C.c_char_p, []),
     "beam_encode": (C.c_int, [i32, i64, P_i64, P_i32, P_i32, P_i32, C.c_char_p, C.POINTER(Encoding)]),
     "beam_exact_partition_cost": (C.c_int, [i32, P_i64, P_i32, P_i32, P_i64]),
     "beam_partition_hash": (u64, [i32, P_i32]),

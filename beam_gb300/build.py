@@ -4,6 +4,8 @@
   beam_gb300/bin/beam          the command-line front end
   oracle/bin/*                 the C oracle (test infrastructure)
   oracle/_ref/beam_ref         the reference program, only where its sources exist
+                               (BEAM_REFERENCE_DIR, else a `reference` checkout
+                               beside this repository)
 
 Translation units compile in parallel; objects are reused when newer than
 their sources and headers.
@@ -24,9 +26,16 @@ BUILD = PKG / "_build"
 LIB = PKG / "libbeam_gb300.so"
 CLI = PKG / "bin" / "beam"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-REFERENCE_DIR = Path("/root/reference")
 
-CU_SOURCES = ["divide.cu", "merge.cu", "engine.cu", "noalloc.cu", "ranker.cu", "partition_cost.cu", "encode_gpu.cu"]
+
+def reference_dir() -> Path:
+    """Where the reference's sources are looked for (they need not exist)."""
+    env = os.environ.get("BEAM_REFERENCE_DIR")
+    return Path(env) if env else ROOT.parent / "reference"
+
+
+CU_SOURCES = ["divide.cu", "merge.cu", "engine.cu", "noalloc.cu", "ranker.cu", "partition_cost.cu", "encode_gpu.cu",
+              "legacy_scoring.cu"]
 CPP_SOURCES = ["graph.cpp", "encode.cpp"]
 
 
@@ -76,7 +85,7 @@ def build_library(jobs: int = 8, verbose: bool = False) -> Path:
         obj = BUILD / (src + ".o")
         objects.append(obj)
         if _stale(obj, [CSRC / src] + headers):
-            tasks.append(["g++", "-std=c++17", "-O3", "-fPIC", "-ffp-contract=off", "-Wall",
+            tasks.append(["g++", "-std=c++17", "-O3", "-fPIC", "-pthread", "-ffp-contract=off", "-Wall",
                           "-I", str(ROOT / "include"), "-c", str(CSRC / src), "-o", str(obj)])
     with ThreadPoolExecutor(max_workers=jobs) as pool:
         list(pool.map(_run, tasks))
@@ -108,15 +117,16 @@ def build_oracle(with_reference: bool | None = None) -> None:
     if _stale(oracle / "bin" / "beam_oracle", deps):
         jobs.append(["gcc", *cflags, "-o", str(oracle / "bin" / "beam_oracle"), str(oracle / "oracle_cli.c"), *src,
                      "-lm"])
+    ref_dir = reference_dir()
     if with_reference is None:
-        with_reference = (REFERENCE_DIR / "src" / "sweg.cpp").exists()
+        with_reference = (ref_dir / "src" / "sweg.cpp").exists()
     if with_reference and not (oracle / "_ref" / "beam_ref").exists():
         (oracle / "_ref").mkdir(exist_ok=True)
         ref_srcs = ["src/main.cpp", "src/sweg.cpp", "src/quotient_graph.cpp", "src/cost_oracle.cpp",
                     "src/scoring_cpu.cpp", "src/candidate_index.cpp", "src/graph_io/graph_io.cpp",
                     "src/cuda_scoring_stub.cpp"]
-        jobs.append(["g++", "-O3", "-std=c++17", "-fopenmp", "-DNDEBUG", f"-I{REFERENCE_DIR / 'include'}", "-o",
-                     str(oracle / "_ref" / "beam_ref"), *[str(REFERENCE_DIR / s) for s in ref_srcs]])
+        jobs.append(["g++", "-O3", "-std=c++17", "-fopenmp", "-DNDEBUG", f"-I{ref_dir / 'include'}", "-o",
+                     str(oracle / "_ref" / "beam_ref"), *[str(ref_dir / s) for s in ref_srcs]])
     with ThreadPoolExecutor(max_workers=3) as pool:
         list(pool.map(_run, jobs))
 

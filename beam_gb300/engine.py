@@ -278,6 +278,51 @@ class Engine:
         return int(out.value)
 
 
+class FlatScorer:
+    """Legacy-objective pair scoring over a flat per-block CSR on the GPU: the
+    service behind the reference's Sweg::ScoreCandidatesCuda
+    (src/cuda_scoring.cu:714-885) with --cost-objective legacy."""
+
+    KEYS = {"offsets": np.int32, "reps": np.int32, "rsz": np.int64, "self": np.int64, "nb": np.int32,
+            "wt": np.int64, "nsz": np.int64}
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        N.check(N.lib().beam_flat_scorer_create(device, C.byref(h)), "beam_flat_scorer_last_error")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            N.lib().beam_flat_scorer_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def score(self, flat: dict, pairs) -> tuple[np.ndarray, np.ndarray]:
+        """{gain, before_cost} per (a_idx, b_idx) row pair, in pair order."""
+        f = {k: np.ascontiguousarray(flat[k], t) for k, t in self.KEYS.items()}
+        pairs = np.ascontiguousarray(np.asarray(pairs, np.int32).reshape(-1, 2))
+        gain = np.zeros(len(pairs), np.int64)
+        before = np.zeros(len(pairs), np.int64)
+        N.check(N.lib().beam_flat_scorer_score(
+            self._h, _ptr(pairs, C.c_int32), len(pairs), _ptr(f["offsets"], C.c_int32), _ptr(f["reps"], C.c_int32),
+            _ptr(f["rsz"], C.c_int64), _ptr(f["self"], C.c_int64), len(f["reps"]), _ptr(f["nb"], C.c_int32),
+            _ptr(f["wt"], C.c_int64), _ptr(f["nsz"], C.c_int64), len(f["nb"]), _ptr(gain, C.c_int64),
+            _ptr(before, C.c_int64)), "beam_flat_scorer_last_error")
+        return gain, before
+
+    def stats(self) -> dict:
+        st = N.FlatScorerStats()
+        N.check(N.lib().beam_flat_scorer_get_stats(self._h, C.byref(st)), "beam_flat_scorer_last_error")
+        return st.as_dict()
+
+
 RANKER_FEATURES = 16
 RANKER_PARAMS = 64 * 16 + 64 + 64 + 1
 

@@ -219,8 +219,12 @@ const char* beam_engine_last_error(void);
  * min(rows*(rows-1)/2, rows*top_k). stream is a cudaStream_t (NULL = legacy
  * default stream); the call waits for its kernel before returning.
  *
- * Limits: rows <= 256, num_entries <= 65536, top_k <= 32; larger requests
- * fail with a message and launch nothing. The scratch is one static device
+ * Limits: rows <= 256, num_entries <= 65536, 1 <= top_k <= 32; other
+ * requests fail with a message and launch nothing. Every weight must lie in
+ * [0, 2^32): the kernel stages counts as 32-bit words, and a call with a
+ * weight outside that range fails with a message (*out_count = -1), as does
+ * one whose offsets do not rise from 0 to num_entries or whose row_rep_ids
+ * repeat. The scratch is one static device
  * array of about 3 MB, resident on every GPU that loads the library until the
  * process exits, shared by all calls: its contents stay from the last call
  * (the kernel clears what must start at zero) and calls that overlap on the
@@ -232,6 +236,41 @@ int beam_prepare_flat_noalloc(const int32_t* offsets, const int32_t* row_rep_ids
                               int32_t* out_a_idx, int32_t* out_b_idx, int64_t out_capacity, int32_t* out_count,
                               void* stream);
 const char* beam_prepare_flat_noalloc_last_error(void);
+
+/* ------------------------------------- legacy-objective flat pair scoring */
+
+/* The scoring service of the reference's CUDA mode with --cost-objective
+ * legacy: Sweg::ScoreCandidatesCuda(pairs, FlatAggCSR, chunk)
+ * (include/sweg.hpp:656-658, src/cuda_scoring.cu:714-885; per-pair
+ * arithmetic of ComputeLocalGainKernel, src/cuda_scoring.cu:282-357). A
+ * scorer owns a stream and device / pinned staging buffers that grow to the
+ * largest call, like the reference's CudaScoringCache
+ * (src/cuda_scoring.cu:369-533). */
+typedef struct beam_flat_scorer beam_flat_scorer;
+
+typedef struct {
+  int64_t calls, kernel_launches, pairs, h2d_bytes, d2h_bytes, max_pairs_per_launch;
+  double kernel_ms;
+} beam_flat_scorer_stats;
+
+int beam_flat_scorer_create(int32_t device, beam_flat_scorer** out);
+void beam_flat_scorer_destroy(beam_flat_scorer* s);
+int beam_flat_scorer_get_stats(const beam_flat_scorer* s, beam_flat_scorer_stats* out);
+/* Device-memory budget for one call of a 64-group block's slice, replacing
+ * Sweg::QueryCudaSliceMemoryBudgetBytes (src/cuda_scoring.cu:684-703): a
+ * quarter of the device's free memory, at most 4 GiB. */
+int beam_flat_scorer_memory_budget(beam_flat_scorer* s, int64_t* bytes);
+/* HOST buffers in and out (the reference's std::vector contents):
+ * pairs = count (a_idx, b_idx) row-index pairs; the FlatAggCSR arrays
+ * (include/sweg.hpp:395-403) with rows + 1 offsets rising from 0 to entries
+ * and each row sorted by neighbour without repeats; gain / before_cost get
+ * one value per pair, in pair order (Sweg::LocalGainResult). The layout is
+ * checked before anything is launched; a violation fails with a message. */
+int beam_flat_scorer_score(beam_flat_scorer* s, const int32_t* pairs, int64_t count, const int32_t* offsets,
+                           const int32_t* row_rep_ids, const int64_t* row_sizes, const int64_t* row_self_loops,
+                           int32_t rows, const int32_t* neighbors, const int64_t* weights,
+                           const int64_t* neighbor_sizes, int64_t entries, int64_t* gain, int64_t* before_cost);
+const char* beam_flat_scorer_last_error(void);
 
 /* ------------------------------------------------------- summary output */
 

@@ -1054,10 +1054,13 @@ static int commit_pairs(beam_oracle* o, const int32_t* keep, const int32_t* remo
 }
 
 /* Sweg::Merge, blocked mode (src/sweg.cpp:953-1145) with the reciprocal
- * threshold 1/(iter+1) (src/sweg.cpp:400-406). */
-int beam_oracle_merge(beam_oracle* o, int iter, int total_iterations) {
-  (void)total_iterations;
+ * threshold 1/(iter+1) (src/sweg.cpp:400-406), over the blocks that start at
+ * group first_group, in order; stops after the block during which budget_ms
+ * of wall time ran out (budget_ms <= 0: no limit). *next_group receives the
+ * first group of the next unprocessed block. */
+static int merge_blocks(beam_oracle* o, int iter, int64_t first_group, double budget_ms, int64_t* next_group) {
   const double threshold = 1.0 / (double)(iter + 1);
+  const double start_ms = now_ms();
   const int64_t bs = o->cfg.group_batch_size;
   prepared* prep = (prepared*)xcalloc((size_t)bs, sizeof(prepared));
   int32_t* items = (int32_t*)xmalloc(sizeof(int32_t) * (size_t)bs);
@@ -1066,7 +1069,9 @@ int beam_oracle_merge(beam_oracle* o, int iter, int total_iterations) {
   int32_t* sr = (int32_t*)xmalloc(sizeof(int32_t) * (size_t)sel_cap);
   int64_t* sg = (int64_t*)xmalloc(sizeof(int64_t) * (size_t)sel_cap);
   int rc = 0;
-  for (int64_t b0 = 0; b0 < o->n_groups && rc == 0; b0 += bs) {
+  int64_t b0 = first_group;
+  for (; b0 < o->n_groups && rc == 0; b0 += bs) {
+    if (budget_ms > 0 && b0 > first_group && now_ms() - start_ms >= budget_ms) break;
     const int64_t b1 = b0 + bs < o->n_groups ? b0 + bs : o->n_groups;
     int32_t nw = 0;
     for (int64_t gi = b0; gi < b1; ++gi) {
@@ -1121,7 +1126,22 @@ int beam_oracle_merge(beam_oracle* o, int iter, int total_iterations) {
   free(sk);
   free(sr);
   free(sg);
+  if (next_group) *next_group = b0 < o->n_groups ? b0 : o->n_groups;
   return rc;
+}
+
+int beam_oracle_merge(beam_oracle* o, int iter, int total_iterations) {
+  (void)total_iterations;
+  return merge_blocks(o, iter, 0, 0.0, NULL);
+}
+
+int beam_oracle_merge_blocks(beam_oracle* o, int iter, int64_t first_group, double budget_ms,
+                             int64_t* next_group) {
+  if (first_group < 0 || first_group > o->n_groups || first_group % o->cfg.group_batch_size != 0) {
+    set_err("first_group must be a block boundary within the iteration's groups");
+    return -1;
+  }
+  return merge_blocks(o, iter, first_group, budget_ms, next_group);
 }
 
 /* Sweg::Run (src/sweg.cpp:651-709). */
@@ -1409,4 +1429,63 @@ int beam_oracle_encode(beam_oracle* o, const char* dir, beam_oracle_encoding* ou
   free(ssize);
   free(shead);
   return rc;
+}
+
+/* ------------------------------------------- legacy-objective flat scoring */
+
+static int64_t legacy_cost(int32_t row_rep, int64_t row_size, int32_t nb_rep, int64_t nb_size, int64_t e) {
+  const int64_t cap = row_rep == nb_rep ? row_size * (row_size - 1) / 2 : row_size * nb_size;
+  const int64_t alt = 1 + cap - e;
+  return e < alt ? e : alt;
+}
+
+typedef struct {
+  int32_t ra, rb;
+  int64_t sa, sb, la, lb;
+  int64_t before, after;
+  int seen_a, seen_b;
+} legacy_acc;
+
+static void legacy_term(legacy_acc* g, int32_t x, int64_t sx, int64_t ea_raw, int64_t eb_raw) {
+  if (x == g->ra) g->seen_a = 1;
+  if (x == g->rb) g->seen_b = 1;
+  int64_t ea = ea_raw, eb = eb_raw;
+  if (x == g->ra) ea = ea_raw > g->la ? ea_raw - g->la : 0;
+  if (x == g->rb) eb = eb_raw > g->lb ? eb_raw - g->lb : 0;
+  g->before += legacy_cost(g->ra, g->sa, x, sx, ea) + legacy_cost(g->rb, g->sb, x, sx, eb);
+  const int64_t sm = g->sa + g->sb;
+  g->after += legacy_cost(g->ra, sm, x == g->rb ? g->ra : x, x == g->rb ? sm : sx, ea + eb);
+}
+
+/* Legacy local gain of rows a and b of a flat per-block CSR, the host check
+ * of the reference's CUDA mode (ComputeLocalGainHostFromFlat,
+ * src/cuda_scoring.cu:146-252): a two-pointer union of the two sorted rows;
+ * every neighbour x adds the costs of (a, x) and (b, x) before and of
+ * (a+b, x) after, counts toward a row's own representative less its
+ * self-loops, and a representative missing from both rows is added with
+ * count 0. */
+int beam_oracle_legacy_flat_gain(const int32_t* offsets, const int32_t* reps, const int64_t* row_sizes,
+                                 const int64_t* self_loops, const int32_t* nb, const int64_t* wt,
+                                 const int64_t* nsz, int32_t a, int32_t b, int64_t* gain, int64_t* before) {
+  legacy_acc g = {reps[a], reps[b], row_sizes[a], row_sizes[b], self_loops[a], self_loops[b], 0, 0, 0, 0};
+  int32_t ia = offsets[a], ib = offsets[b];
+  const int32_t ea = offsets[a + 1], eb = offsets[b + 1];
+  while (ia < ea || ib < eb) {
+    if (ib >= eb || (ia < ea && nb[ia] < nb[ib])) {
+      legacy_term(&g, nb[ia], nsz[ia], wt[ia], 0);
+      ++ia;
+    } else if (ia >= ea || nb[ib] < nb[ia]) {
+      legacy_term(&g, nb[ib], nsz[ib], 0, wt[ib]);
+      ++ib;
+    } else {
+      legacy_term(&g, nb[ia], nsz[ia], wt[ia], wt[ib]);
+      ++ia;
+      ++ib;
+    }
+  }
+  if (!g.seen_a) legacy_term(&g, g.ra, g.sa, 0, 0);
+  if (g.rb != g.ra && !g.seen_b) legacy_term(&g, g.rb, g.sb, 0, 0);
+  *gain = g.before - g.after;
+  *before = g.before;
+  return 0;
 }

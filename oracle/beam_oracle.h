@@ -65,6 +65,12 @@ const char* beam_oracle_last_error(void);
 int beam_oracle_run(beam_oracle* o, int iterations);
 int beam_oracle_divide(beam_oracle* o, int iter);
 int beam_oracle_merge(beam_oracle* o, int iter, int total_iterations);
+/* The blocks of Merge(iter) that start at group first_group (a block
+ * boundary), in order, until budget_ms of wall time has run out at a block
+ * boundary (budget_ms <= 0: to the end): a bounded sample of an iteration for
+ * timing. *next_group = the first group of the next unprocessed block. */
+int beam_oracle_merge_blocks(beam_oracle* o, int iter, int64_t first_group, double budget_ms,
+                             int64_t* next_group);
 
 /* Divide output: order[] holds the active reps in group order (length =
  * active count), starts[] the group starts (length = group count). */
@@ -94,6 +100,13 @@ int64_t beam_oracle_internal(const beam_oracle* o, int32_t rep);
 int64_t beam_oracle_row(const beam_oracle* o, int32_t rep, int32_t* nb, int64_t* cnt, int64_t cap);
 int64_t beam_oracle_exact_partition_cost(const beam_oracle* o);
 void beam_oracle_get_stats(const beam_oracle* o, beam_oracle_stats* out);
+
+/* Legacy-objective local gain of rows a and b of a flat per-block CSR
+ * (Sweg::FlatAggCSR), as the reference's CUDA mode scores pairs
+ * (src/cuda_scoring.cu:146-252, 282-357). */
+int beam_oracle_legacy_flat_gain(const int32_t* offsets, const int32_t* reps, const int64_t* row_sizes,
+                                 const int64_t* self_loops, const int32_t* nb, const int64_t* wt,
+                                 const int64_t* nsz, int32_t a, int32_t b, int64_t* gain, int64_t* before);
 
 /* Sweg::Encode + ComputeCompressionMetrics (mags-compatible). When dir is not
  * NULL, writes G.txt / P.txt / Cp.txt / Cm.txt there. */

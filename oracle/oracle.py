@@ -68,6 +68,7 @@ def lib() -> C.CDLL:
             "beam_oracle_run": (C.c_int, [vp, C.c_int]),
             "beam_oracle_divide": (C.c_int, [vp, C.c_int]),
             "beam_oracle_merge": (C.c_int, [vp, C.c_int, C.c_int]),
+            "beam_oracle_merge_blocks": (C.c_int, [vp, C.c_int, i64, C.c_double, P64]),
             "beam_oracle_group_count": (i64, [vp]),
             "beam_oracle_active_count": (i64, [vp]),
             "beam_oracle_groups": (C.c_int, [vp, P32, P32, P32]),
@@ -84,6 +85,7 @@ def lib() -> C.CDLL:
             "beam_oracle_exact_partition_cost": (i64, [vp]),
             "beam_oracle_get_stats": (None, [vp, C.POINTER(OracleStats)]),
             "beam_oracle_encode": (C.c_int, [vp, C.c_char_p, C.POINTER(OracleEncoding)]),
+            "beam_oracle_legacy_flat_gain": (C.c_int, [P32, P32, P64, P64, P32, P64, P64, i32, i32, P64, P64]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -138,6 +140,17 @@ class Oracle:
 
     def merge(self, it, total=20):
         self._check(lib().beam_oracle_merge(self._h, it, total))
+
+    def merge_blocks(self, it, first_group=0, budget_ms=0.0) -> int:
+        """The blocks of Merge(it) from group first_group (a block boundary)
+        until budget_ms ran out (<= 0: to the end); returns the first group of
+        the next unprocessed block."""
+        nxt = C.c_int64()
+        self._check(lib().beam_oracle_merge_blocks(self._h, it, int(first_group), float(budget_ms), C.byref(nxt)))
+        return int(nxt.value)
+
+    def group_count(self) -> int:
+        return int(lib().beam_oracle_group_count(self._h))
 
     def groups(self):
         na = lib().beam_oracle_active_count(self._h)
@@ -210,3 +223,22 @@ class Oracle:
         self._check(lib().beam_oracle_encode(self._h, None if out_dir is None else str(out_dir).encode(),
                                              C.byref(enc)))
         return {n: getattr(enc, n) for n, _ in enc._fields_}
+
+
+def legacy_flat_gains(flat: dict, pairs) -> tuple[np.ndarray, np.ndarray]:
+    """Legacy-objective {gain, before_cost} of (a_idx, b_idx) row pairs of a flat
+    per-block CSR (keys offsets, reps, rsz, self, nb, wt, nsz)."""
+    f = {k: np.ascontiguousarray(flat[k], np.int64 if k in ("rsz", "self", "wt", "nsz") else np.int32)
+         for k in ("offsets", "reps", "rsz", "self", "nb", "wt", "nsz")}
+    pairs = np.asarray(pairs, np.int32).reshape(-1, 2)
+    gain = np.zeros(len(pairs), np.int64)
+    before = np.zeros(len(pairs), np.int64)
+    g, b = C.c_int64(), C.c_int64()
+    L = lib()
+    for i, (x, y) in enumerate(pairs.tolist()):
+        L.beam_oracle_legacy_flat_gain(_p(f["offsets"], C.c_int32), _p(f["reps"], C.c_int32),
+                                       _p(f["rsz"], C.c_int64), _p(f["self"], C.c_int64), _p(f["nb"], C.c_int32),
+                                       _p(f["wt"], C.c_int64), _p(f["nsz"], C.c_int64), x, y, C.byref(g),
+                                       C.byref(b))
+        gain[i], before[i] = g.value, b.value
+    return gain, before

@@ -130,3 +130,29 @@ def test_summary_is_lossless(case, tmp_path):
     u, v = g.edge_list()
     want = {(min(a, b), max(a, b)) for a, b in zip(u.tolist(), v.tolist())}
     assert reconstruct(tmp_path) == want
+
+
+def test_merge_blocks_resume_at_block_boundaries():
+    """The bounded timing sample (Merge's blocks from a block boundary, until a
+    time budget runs out) ends at a block boundary, and samples that resume
+    where the last one ended give the whole Merge."""
+    from beam_gb300 import Graph
+    g = Graph.generate("rmat:scale=12,ef=4,a=0.57,b=0.19,c=0.19,seed=3")
+    full = Oracle.from_graph(g, threads=2, group_batch_size=8)
+    part = Oracle.from_graph(g, threads=2, group_batch_size=8)
+    full.divide(1)
+    full.merge(1)
+    part.divide(1)
+    ngroups = len(part.groups()[1])
+    at, steps = 0, 0
+    while at < ngroups:
+        nxt = part.merge_blocks(1, at, 1e-9)  # the budget is spent after one block
+        assert nxt == min(at + 8, ngroups)
+        at, steps = nxt, steps + 1
+    assert steps == (ngroups + 7) // 8
+    assert part.partition_hash() == full.partition_hash()
+    assert part.stats()["accepted_merges_after_validation"] == full.stats()["accepted_merges_after_validation"]
+    with pytest.raises(RuntimeError, match="block boundary"):
+        part.merge_blocks(1, 3, 0.0)
+    for o in (full, part):
+        o.close()
