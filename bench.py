@@ -1,20 +1,25 @@
 #!/usr/bin/env python
-"""Benchmark of the GB300 merge loop on the R-MAT scale-19 workload.
+"""Benchmark of the GB300 merge loop on R-MAT scale 24, edge factor 16 (the
+large single-GPU configuration: n = 16.8M, m = 260M, 521M CSR arcs).
 
 A step is one full 20-iteration run of the merge loop (Divide + Merge, the
 reference's runtime_run_ms span) over the resident graph. The quotient graph
 is reset to singletons and L2 is flushed (256 MB write) before every timed
 step; both stay outside the timed span, which is measured with CUDA events on
 the engine's stream. value = accepted merges of all ranks / slowest rank's
-time for the headline form (--form, default batched: one block of all groups
-per iteration); the other forms (plain: the reference's 64-group blocks,
-bit-exact with the reference; ranker: batched + the learned candidate
-ranker) are timed beside it for the speed-ups and the cost-ratio comparison.
-e2e runs the public C ABI from host buffers every step (create from the host
-CSR = H2D copies, 20 iterations, partition download = D2H).
+time for the headline form (--form); the other forms (batched: one block of
+all groups per iteration; ranker: batched + the learned candidate ranker;
+plain: the reference's 64-group blocks, bit-exact with the reference) are
+timed beside it for the speed-ups and the cost-ratio comparison. e2e runs the
+public C ABI from pinned host buffers every step (create from the host CSR =
+H2D copies, 20 iterations, partition download = D2H).
 
---impl reference times the CPU implementation of the path (the C oracle,
-a restatement of the reference pinned to its outputs) on the host cores.
+The CPU side (cpu_baseline, and --impl reference) times the C oracle, a
+restatement of the reference path pinned to the reference's outputs, with
+OpenMP on all host cores (OMP_PROC_BIND=close, OMP_PLACES=cores), on bounded
+samples of the same workload: consecutive 64-group blocks of Merge, each
+sample charged its share of the iteration's Divide time. A full 20-iteration
+CPU run of this graph takes hours.
 
 Multi-GPU (torchrun): replicas only - every rank runs the same workload on
 its own GPU with no collective on the data path.
@@ -39,7 +44,11 @@ METRIC = "20-iter wall s & merges/s: batched+ranker vs plain GPU at equal cost r
 UNIT = "merges/s"
 ITERATIONS = 20
 WORKLOAD_DESC = {
+    "rmat24": "R-MAT scale 24, edge factor 16 (a=0.57, b=0.19, c=0.19), seed 11, deduplicated, loop-free",
     "rmat19": "R-MAT scale 19, edge factor 2 (a=0.57, b=0.19, c=0.19), seed 7, deduplicated, loop-free",
+    "rmat20_ef16": "R-MAT scale 20, edge factor 16 (a=0.57, b=0.19, c=0.19), seed 11, deduplicated, loop-free",
+    "chunglu4m_twins": "Chung-Lu n=4M, power-law 2.3, mean degree 17, + 200k planted near-twin groups, seed 4",
+    "grid_chunglu_union": "1400x1400 grid (10% deleted, 2% diagonals) + Chung-Lu n=1.1M, power-law 2.1, seed 3",
     "dcsbm_4096": "degree-corrected SBM n=4096, 32 blocks, p_in/p_out=40, power-law 2.5, mean degree 43, seed 1",
 }
 FALLBACK_HBM_GBS = 6800.0
@@ -266,13 +275,33 @@ def pinned_graph(g):
         return g  # no CUDA-enabled torch: pageable host memory
 
 
-def final_cost_ratio(e, g) -> tuple[float, str]:
+def final_metrics(e) -> tuple[float, str]:
+    """Cost ratio (device Encode) and partition hash of the engine's current
+    partition."""
     from beam_gb300 import partition_hash
 
-    e.reset()
-    e.run(ITERATIONS)
-    labels, head, nxt = e.partition()
-    return g.encode(head, nxt)["cost_ratio_mags_compatible"], str(partition_hash(labels))
+    enc = e.encode()
+    labels, _, _ = e.partition()
+    return enc["cost_ratio_mags_compatible"], str(partition_hash(labels))
+
+
+def hbm_residency(e, g) -> dict:
+    """Device bytes of the resident state, by part (the engine's own buffers)."""
+    n, arcs = g.n, g.arcs
+    pool = 2 * 8 * (3 * arcs + 2 * n + 4096)
+    return {"csr_bytes": 8 * (n + 1) + 8 * arcs, "quotient_pool_bytes": pool,
+            "quotient_row_meta_bytes": 8 * n + 4 * n * 3 + 8 * n,
+            "candidate_bytes_per_slot": 40, "device_used_bytes": device_used_bytes()}
+
+
+def device_used_bytes() -> int | None:
+    try:
+        import torch
+
+        free, total = torch.cuda.mem_get_info()
+        return int(total - free)
+    except Exception:  # noqa: BLE001 - reporting only
+        return None
 
 
 def run_ours(args, dist: Dist) -> dict | None:
@@ -293,8 +322,8 @@ def run_ours(args, dist: Dist) -> dict | None:
         e.reset()
         e.run(ITERATIONS)
     breakdown = kernel_breakdown(e)
-    # the roofline kernel: ScoreKernel, the largest single kernel of the run
-    # (the prepare class is larger in total but spans six kernels and a sort)
+    residency = hbm_residency(e, g)
+    # the roofline kernel: ScoreKernel, the scoring kernel of the path
     dominant = args.timed_kernel or "score"
     dist.barrier()
     e.synchronize()
@@ -310,23 +339,33 @@ def run_ours(args, dist: Dist) -> dict | None:
     all_merges = dist.reduce(float(t["merges"]), "sum")
     value = all_merges / (max_ms / 1000.0)
     ms_per_step = max_ms / args.steps
-    head_ratio, head_hash = final_cost_ratio(e, g)
+    head_ratio, head_hash = final_metrics(e)
+    info = e.ranker_info() if FORMS[head_form].get("ranker") else None
     e.close()
     forms = {head_form: {"wall_s_20iter": round(ms_per_step / 1000.0, 4),
                          "merges_per_s": round(value / dist.world, 1),
                          "merges_per_step": t["merges"] // max(1, args.steps),
                          "cost_ratio_mags_compatible": round(head_ratio, 6),
-                         "partition_hash": head_hash, **FORMS[head_form]}}
+                         "partition_hash": head_hash, "steps": args.steps, **FORMS[head_form]}}
+    if info:
+        forms[head_form]["ranker"] = {k: info[k] for k in ("samples", "train_steps", "ranked", "pruned", "train_ms",
+                                                           "final_loss")}
 
     # the other forms, for the speed-ups and the cost-ratio comparison
     for other_form in others:
         eo = form_engine(g, device, other_form)
-        eo.reset()
-        eo.run(ITERATIONS)
-        o_steps = max(1, min(args.steps, 3))
+        if other_form == "plain":
+            # warm-up: the first iteration sizes every buffer
+            eo.divide(1)
+            eo.merge(1, ITERATIONS)
+            o_steps = max(1, args.plain_steps)
+        else:
+            eo.reset()
+            eo.run(ITERATIONS)
+            o_steps = max(1, min(args.steps, 3))
         to = timed_steps(eo, o_steps, None)
         o_ms = sum(to["step_ms"]) / o_steps
-        o_ratio, o_hash = final_cost_ratio(eo, g)
+        o_ratio, o_hash = final_metrics(eo)  # the partition of the last timed run
         info = eo.ranker_info() if FORMS[other_form].get("ranker") else None
         eo.close()
         forms[other_form] = {"wall_s_20iter": round(o_ms / 1000.0, 4),
@@ -351,14 +390,15 @@ def run_ours(args, dist: Dist) -> dict | None:
     # e2e through the C ABI from host buffers: create from the host CSR
     # held in pinned memory (H2D), 20 iterations, partition download (D2H)
     hg = pinned_graph(g)
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
     e2e_ms, e2e_merges = [], 0
-    for i in range(args.warmup + args.steps):
+    for i in range(1 + e2e_steps):
         t1 = time.perf_counter()
         with form_engine(hg, device, head_form) as ee:
             ee.run(ITERATIONS)
             ee.partition()
             m = ee.stats()["accepted_merges_after_validation"]
-        if i >= args.warmup:
+        if i >= 1:
             e2e_ms.append((time.perf_counter() - t1) * 1000.0)
             e2e_merges += m
     e2e_max = dist.reduce(sum(e2e_ms), "max")
@@ -390,8 +430,10 @@ def run_ours(args, dist: Dist) -> dict | None:
             "flags": "batch-ea-blocked, mags-compatible, persistent, incremental, legacy index, certification off, "
                      "g0, top-k 16, reciprocal threshold, 20 iterations, seed 1",
             "wall_s_20iter": round(ms_per_step / 1000.0, 4),
-            "l2": "flushed by a 256 MB write before every timed step (outside the timed span)",
+            "l2": "flushed by a 256 MB write before every timed step (outside the timed span); the quotient graph "
+                  "(tens of GB) is far larger than L2",
             "parallelism": f"replicas x{dist.world}",
+            "hbm_residency": residency,
         },
         "forms": forms,
         "comparison": comparison,
@@ -401,7 +443,8 @@ def run_ours(args, dist: Dist) -> dict | None:
             "h2d_bytes_per_step": 8 * (g.n + 1) + 4 * g.arcs,
             "host_buffers": "pinned" if isinstance(hg, PinnedGraph) else "pageable",
             "d2h_bytes_per_step": 12 * g.n,
-            "ms_per_step": round(e2e_max / max(1, args.steps), 3),
+            "ms_per_step": round(e2e_max / e2e_steps, 3),
+            "steps": e2e_steps,
         },
         "gpu_launches": t["launches"],
         "roofline": {
@@ -422,62 +465,144 @@ def run_ours(args, dist: Dist) -> dict | None:
         "wall_s_timed_region": round(wall_s, 3),
     }
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        result["cpu_baseline"] = cpu_baseline(g, args)
+        result["cpu_baseline"] = cpu_baseline(args)
     return result
 
 
 # ------------------------------------------------------------ CPU side
 
+OMP_ENV = {"OMP_PROC_BIND": "close", "OMP_PLACES": "cores"}
 
-def cpu_baseline(g, args) -> dict:
-    """The oracle (C restatement of the reference path, OpenMP) on the host
-    cores: one full 20-iteration run of the same workload."""
+
+def host_cpu() -> dict:
+    """Host cores and model (lscpu), for the CPU baseline's description."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"cores": os.cpu_count() or 1, "model": model}
+
+
+def cpu_sample(g, steps: int, warmup: int, step_budget_s: float, threads: int) -> dict:
+    """The oracle on bounded samples of the workload: consecutive 64-group
+    blocks of Merge from iteration 1 on (a step = the blocks that start before
+    step_budget_s has run out, across iteration boundaries), each block charged
+    its groups' share of its iteration's Divide time."""
     sys.path.insert(0, str(ROOT / "oracle"))
     from oracle import Oracle
 
-    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
     o = Oracle.from_graph(g, ea_use_threshold=True, threads=threads)
-    t = time.perf_counter()
-    o.run(ITERATIONS)
-    secs = time.perf_counter() - t
-    merges = o.stats()["accepted_merges_after_validation"]
+    setup_s = time.perf_counter() - t0
+    state = {"it": 1, "at": 0}
+    t1 = time.perf_counter()
+    o.divide(1)
+    state["divide_s"] = time.perf_counter() - t1
+    state["ngroups"] = o.group_count()
+    timed_merges, timed_s, timed_groups, iters = 0, 0.0, 0, set()
+    for step in range(warmup + steps):
+        merges, secs, groups = 0, 0.0, 0
+        while secs < step_budget_s:
+            if state["at"] >= state["ngroups"]:
+                if state["it"] == ITERATIONS:
+                    # the whole run is done: a fresh run of the same graph goes on
+                    o.close()
+                    o = Oracle.from_graph(g, ea_use_threshold=True, threads=threads)
+                    state["it"] = 0
+                state["it"] += 1
+                state["at"] = 0
+                t3 = time.perf_counter()
+                o.divide(state["it"])
+                state["divide_s"] = time.perf_counter() - t3
+                state["ngroups"] = o.group_count()
+                continue
+            m0 = o.stats()["accepted_merges_after_validation"]
+            t2 = time.perf_counter()
+            nxt = o.merge_blocks(state["it"], state["at"], 1000.0 * (step_budget_s - secs))
+            dt = time.perf_counter() - t2
+            secs += dt + state["divide_s"] * (nxt - state["at"]) / max(1, state["ngroups"])
+            merges += o.stats()["accepted_merges_after_validation"] - m0
+            groups += nxt - state["at"]
+            if step >= warmup:
+                iters.add(state["it"])
+            state["at"] = nxt
+        if step >= warmup:
+            timed_merges += merges
+            timed_s += secs
+            timed_groups += groups
     o.close()
-    return {"value": round(merges / secs, 1), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"one full {ITERATIONS}-iteration run of {args.workload} ({merges} merges, {secs:.2f} s)"}
+    return {"merges": timed_merges, "secs": timed_s, "groups": timed_groups, "iterations": sorted(iters),
+            "setup_s": setup_s}
+
+
+def reexec_with_omp_env() -> None:
+    """OpenMP reads its placement variables when it starts: run this process
+    again with them set (once)."""
+    if all(os.environ.get(k) == v for k, v in OMP_ENV.items()):
+        return
+    env = dict(os.environ, **OMP_ENV)
+    env.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    os.execve(sys.executable, [sys.executable, *sys.argv], env)
+
+
+def cpu_baseline(args) -> dict:
+    """The oracle on the host cores in a child process (OpenMP placement set
+    before it starts), one bounded sample of the workload."""
+    cmd = [sys.executable, str(ROOT / "bench.py"), "--cpu-sample", "--workload", args.workload,
+           "--sample-seconds", str(args.cpu_sample_seconds)]
+    env = dict(os.environ, **OMP_ENV, OMP_NUM_THREADS=str(os.cpu_count() or 1))
+    proc = subprocess.run(cmd, capture_output=True, text=True, env=env)
+    lines = [l for l in proc.stdout.splitlines() if l.startswith("{")]
+    if proc.returncode != 0 or not lines:
+        return {"value": None, "unit": UNIT, "cores": 0, "kind": "port",
+                "sample": f"CPU sample failed: {proc.stderr[-300:]}"}
+    return json.loads(lines[-1])
+
+
+def cpu_sample_main(args) -> None:
+    from beam_gb300 import WORKLOADS, Graph
+
+    g = Graph.generate(WORKLOADS[args.workload])
+    cpu = host_cpu()
+    r = cpu_sample(g, steps=1, warmup=0, step_budget_s=args.sample_seconds, threads=cpu["cores"])
+    value = r["merges"] / r["secs"] if r["secs"] > 0 else 0.0
+    print(json.dumps({
+        "value": round(value, 1), "unit": UNIT, "cores": cpu["cores"], "kind": "port",
+        "affinity": "OMP_PROC_BIND=close, OMP_PLACES=cores", "cpu_model": cpu["model"],
+        "sample": f"the C oracle (the reference path restated, pinned to its outputs) on {args.workload}: the first "
+                  f"{r['groups']} Divide groups of iteration(s) {r['iterations']} in 64-group blocks "
+                  f"({r['merges']} merges, {r['secs']:.2f} s including their share of Divide; oracle setup "
+                  f"{r['setup_s']:.1f} s untimed)"}), flush=True)
 
 
 def run_reference(args, dist: Dist) -> dict | None:
     if dist.rank != 0:
         return None
-    sys.path.insert(0, str(ROOT / "oracle"))
-    from oracle import Oracle
-
     from beam_gb300 import WORKLOADS, Graph
 
     g = Graph.generate(WORKLOADS[args.workload])
-    threads = os.cpu_count() or 1
-    times, merges = [], 0
-    for i in range(args.warmup + args.steps):
-        o = Oracle.from_graph(g, ea_use_threshold=True, threads=threads)
-        t = time.perf_counter()
-        o.run(ITERATIONS)
-        dt = time.perf_counter() - t
-        m = o.stats()["accepted_merges_after_validation"]
-        o.close()
-        if i >= args.warmup:
-            times.append(dt)
-            merges += m
-    value = merges / sum(times)
+    cpu = host_cpu()
+    budget = args.reference_step_seconds
+    r = cpu_sample(g, steps=args.steps, warmup=args.warmup, step_budget_s=budget, threads=cpu["cores"])
+    value = r["merges"] / r["secs"] if r["secs"] > 0 else 0.0
+    sample = (f"consecutive 64-group blocks of Merge from iteration 1 on, about {budget:g} s per step "
+              f"({args.warmup} warm-up + {args.steps} timed steps, {r['groups']} Divide groups of iteration(s) "
+              f"{r['iterations']} timed, each step charged its groups' share of Divide)")
     return {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(1000.0 * sum(times) / args.steps, 3), "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": round(1000.0 * r["secs"] / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic (seeded generator)",
         "impl": "reference",
         "config": {"workload": f"{args.workload}: {WORKLOAD_DESC.get(args.workload, '')}; n={g.n}, m={g.edges}",
                    "path": "CPU restatement of the reference path (C + OpenMP), pinned bit-exact to its outputs",
-                   "wall_s_20iter": round(sum(times) / args.steps, 4)},
-        "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"one full {ITERATIONS}-iteration run per step"},
+                   "affinity": "OMP_PROC_BIND=close, OMP_PLACES=cores", "cpu_model": cpu["model"]},
+        "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": cpu["cores"], "kind": "port",
+                         "sample": sample},
         "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -490,7 +615,7 @@ def profile_run(args) -> None:
     batch = FORMS[args.form]["group_batch_size"]
     with Engine(g, ea_use_threshold=True, **FORMS[args.form]) as e:
         t = time.perf_counter()
-        e.run(ITERATIONS)
+        e.run(args.profile_iterations)
         e.synchronize()
         st = e.stats()
         log(f"[profile-run] {args.workload} batch={batch}: {time.perf_counter() - t:.3f} s, "
@@ -502,18 +627,27 @@ def profile_run(args) -> None:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile-run", action="store_true", help="one run only, for ncu")
+    ap.add_argument("--profile-iterations", type=int, default=ITERATIONS)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="rmat19")
+    ap.add_argument("--workload", default="rmat24")
     ap.add_argument("--timed-kernel", choices=list(KERNEL_CLASSES), default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--form", choices=list(FORMS), default="batched",
                     help="form whose throughput is the headline value")
     ap.add_argument("--no-other-form", action="store_true", help="skip timing the other forms")
+    ap.add_argument("--plain-steps", type=int, default=1, help="timed runs of the plain form")
+    ap.add_argument("--e2e-steps", type=int, default=5, help="timed e2e runs (at most --steps)")
     ap.add_argument("--batch-groups", type=int, default=None,
                     help="groups per block of the batched and ranker forms (default: all groups of an iteration)")
+    ap.add_argument("--cpu-sample", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--sample-seconds", type=float, default=20.0, help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-sample-seconds", type=float, default=20.0,
+                    help="length of the CPU baseline's bounded sample")
+    ap.add_argument("--reference-step-seconds", type=float, default=4.0,
+                    help="length of one step of the reference arm's bounded samples")
     args = ap.parse_args()
     if args.batch_groups:
         for f in ("batched", "ranker"):
@@ -521,8 +655,13 @@ def main():
     if args.profile_run:
         profile_run(args)
         return
+    if args.cpu_sample:
+        cpu_sample_main(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
+    if args.impl == "reference" and int(os.environ.get("RANK", "0")) == 0:
+        reexec_with_omp_env()
     dist = Dist()
     try:
         result = run_reference(args, dist) if args.impl == "reference" else run_ours(args, dist)
