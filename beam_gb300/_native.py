@@ -130,6 +130,7 @@ SIGNATURES = {
     "beam_engine_get_stats": (C.c_int, [vp, C.POINTER(EngineStats)]),
     "beam_engine_quotient_nnz": (C.c_int, [vp, P_i64]),
     "beam_engine_exact_partition_cost": (C.c_int, [vp, P_i64]),
+    "beam_engine_validate_quotient": (C.c_int, [vp]),
     "beam_engine_encode": (C.c_int, [vp, C.c_char_p, C.POINTER(Encoding)]),
     "beam_engine_ranker_info": (C.c_int, [vp, C.POINTER(RankerInfo)]),
     "beam_ranker_grad": (C.c_int, [i32, vp, vp, vp, i64, vp, vp, P_f64, vp]),

@@ -748,6 +748,10 @@ int beam_engine_exact_partition_cost(beam_engine* e, int64_t* cost) {
   return Guard([&] { *cost = e->impl->ExactPartitionCost(); });
 }
 
+int beam_engine_validate_quotient(beam_engine* e) {
+  return Guard([&] { e->impl->ValidateQuotient(); });
+}
+
 int beam_engine_quotient_nnz(beam_engine* e, int64_t* nnz) {
   return Guard([&] { *nnz = e->impl->QuotientNnz(); });
 }

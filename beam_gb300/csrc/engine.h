@@ -193,6 +193,8 @@ class Engine {
   int64_t QuotientNnz();
   // CostOracle::ExactPartitionCost of the current partition, from the input graph.
   int64_t ExactPartitionCost();
+  // QuotientGraph::ValidateAgainstOriginalGraph: throws on the first mismatch.
+  void ValidateQuotient();
   // Sweg::Encode of the current partition: P (supernode ids), Cp and Cm.
   void Encode(EncodeOutput* out);
   const HostStats& host_stats() const { return hstats_; }

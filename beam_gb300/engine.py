@@ -216,6 +216,11 @@ class Engine:
         N.check(N.lib().beam_engine_exact_partition_cost(self._h, C.byref(out)))
         return int(out.value)
 
+    def validate_quotient(self) -> None:
+        """QuotientGraph::ValidateAgainstOriginalGraph on the device: raises
+        BeamError on the first difference from a full rebuild."""
+        N.check(N.lib().beam_engine_validate_quotient(self._h))
+
     def ranker_info(self) -> dict:
         info = N.RankerInfo()
         N.check(N.lib().beam_engine_ranker_info(self._h, C.byref(info)))

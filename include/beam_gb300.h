@@ -185,6 +185,12 @@ const char* beam_ranker_last_error(void);
  * engine's current partition, computed on the device from the resident input
  * graph (sort of supernode-pair keys + run-length encode); the check of
  * src/main.cpp:560-566 compares it with the encoding payload. */
+/* QuotientGraph::ValidateAgainstOriginalGraph (src/quotient_graph.cpp:867-886),
+ * --validate-quotient: the resident quotient graph (sizes, internal counts,
+ * every row) against a full rebuild from the current labels, and its exact
+ * cost against CostOracle::ExactPartitionCost. Fails with the reference's
+ * message on the first mismatch. */
+int beam_engine_validate_quotient(beam_engine* e);
 int beam_engine_exact_partition_cost(beam_engine* e, int64_t* cost);
 /* QuotientGraph::Nnz (src/quotient_graph.cpp:259-270). */
 int beam_engine_quotient_nnz(beam_engine* e, int64_t* nnz);

@@ -184,3 +184,19 @@ def test_batched_form_matches_oracle(name):
             assert st[k] == ost[k], k
     assert 1 <= st["blocks"] <= 20
     e.close()
+
+
+@pytest.mark.parametrize("batch", [64, 1 << 30])
+def test_validate_quotient_after_every_iteration(batch):
+    """--validate-quotient: after every Merge the resident quotient graph equals
+    a full rebuild from the labels (QuotientGraph::ValidateAgainstOriginalGraph,
+    src/quotient_graph.cpp:867-886), in the plain and the batched forms."""
+    from beam_gb300 import Engine, Graph
+    for spec in ("rmat:scale=12,ef=4,a=0.57,b=0.19,c=0.19,seed=3", "dcsbm:n=4096,blocks=32,ratio=40,gamma=2.5,deg=43,seed=1"):
+        g = Graph.generate(spec)
+        with Engine(g, group_batch_size=batch) as e:
+            e.validate_quotient()
+            for it in range(1, 8):
+                e.divide(it)
+                e.merge(it, 20)
+                e.validate_quotient()
