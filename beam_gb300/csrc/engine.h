@@ -352,6 +352,7 @@ class Engine {
   DevBuf<unsigned short> d_rk_wbf_;
   DevBuf<double> d_rk_npartial_;
   DevBuf<float> d_rk_zbuf_, d_rk_zpos_[2], d_rk_cut_;  // per-slot logits, exploration positives, cutoff
+  DevBuf<long long> d_rk_zgain_[2];                    // exact gains of the exploration positives
   bool rk_trained_ = false;
   float rk_cutoff_ = 0.0f;
   long long rk_iter_slots_ = 0;

@@ -751,85 +751,113 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareKernel(PrepareParams P) {
   }
 }
 
-// Fill pass of the deferred groups, grid (big-group entry, slice): one
-// thread per row entry of the group (entries of one member are contiguous,
-// found by a binary search of the row offsets staged in shared memory), so a
-// hub member's long row is spread over many warps. Per entry: its sort key
-// (launch-local group index, target) and value (member, count), the entry's
-// approximate-old-cost term (summed per member by a
-// segmented warp scan, one atomic per member run), and direct in-group edges,
-// which go to both halves of the pair table (row i holds j and row j holds i
-// with the same count), so no mirror pass is needed.
+// Fill pass of the deferred groups: one thread per sort slot of the launch
+// (the groups' slot ranges, soff, laid end to end), CTAs striding over windows
+// of kFillWindow slots, so the grid follows the total row entries and a hub
+// member's long row is spread over many warps. A window's first group is
+// found by a binary search of soff; each lane walks forward from it, and
+// finds its member by a binary search of the group's row offsets (entries of
+// one member are contiguous). Per entry: its sort key (launch-local group
+// index, target) and value (member, count), the entry's approximate-old-cost
+// term (summed per member run by a segmented warp scan, one atomic per run),
+// and direct in-group edges, which go to both halves of the pair table (row i
+// holds j and row j holds i with the same count), so no mirror pass is
+// needed. Slots past a group's entries keep the padding key.
 constexpr int kFillThreads = 256;
+constexpr int kFillWindow = 2048;
 constexpr int kAccumThreads = 256;
 
 __global__ void __launch_bounds__(kFillThreads) PrepareFillKernel(PrepareParams P) {
-  __shared__ int eoff_s[kMaxGroup + 1];
-  const BigDesc d = P.desc[P.list0 + blockIdx.x];
-  if (d.base == nullptr) return;
+  __shared__ int first_group;
   const int lane = threadIdx.x & 31;
-  const int ri = P.list[P.list0 + blockIdx.x];
-  const int gid = P.real[ri];
-  const int g = P.glen[gid];
-  const long long gg = static_cast<long long>(g) * g;
-  unsigned char* mat = P.mat + P.mat_off[ri];
-  long long* pmat = reinterpret_cast<long long*>(mat);
-  unsigned long long* old_out = reinterpret_cast<unsigned long long*>(mat + OldCostOffset(gg));
-  const DeferredView V = Deferred(d.base, g);
-  const long long slot = P.soff[P.list0 + blockIdx.x] - P.slot0;
-  const unsigned long long key_hi = static_cast<unsigned long long>(blockIdx.x) << P.tbits;
-  for (int i = threadIdx.x; i <= g; i += kFillThreads) eoff_s[i] = V.eoff[i];
-  __syncthreads();
   const QuotientView& Q = P.Q;
-  const int stride = gridDim.y * kFillThreads;
-  for (int base = blockIdx.y * kFillThreads; base < d.E; base += stride) {
-    const int idx = base + threadIdx.x;
-    int i = -1;
-    long long cost = 0, light = 0;
-    if (idx < d.E) {
-      int lo = 0, hi = g;  // last member with eoff <= idx
+  const long long windows = (P.nslots + kFillWindow - 1) / kFillWindow;
+  for (long long w = blockIdx.x; w < windows; w += gridDim.x) {
+    const long long w0 = w * kFillWindow;
+    if (threadIdx.x == 0) {
+      int lo = 0, hi = P.nlist;  // last group whose slot range starts at or before w0
       while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
-        if (eoff_s[mid] <= idx) lo = mid; else hi = mid;
+        if (P.soff[P.list0 + mid] - P.slot0 <= w0) lo = mid; else hi = mid;
       }
-      i = lo;
-      const int rep = V.mq[i];
-      const Entry e = Q.ent[Q.off[rep] + (idx - eoff_s[i])];
-      const int t = EntNb(e);
-      const long long c = EntCnt(e);
-      const long long st = Q.size[t];
-      cost = EncodeCostForPair(rep, V.msz[i], t, st, c);
-      if (P.rc_before) {
-        if (HeavyEntry(V.msz[i], st, c)) {
-          const int rank = atomicAdd(&P.rc_nheavy[rep], 1);
-          if (rank < kHeavyMax) reinterpret_cast<int*>(&P.rc_heavy[rep])[rank] = idx - eoff_s[i];
-        } else {
-          light = c;
+      first_group = lo;
+    }
+    __syncthreads();
+    int k = first_group;
+    int i = -1;  // member of the previous slot (same group), -1 none
+    for (int off = threadIdx.x; off < kFillWindow; off += kFillThreads) {
+      const long long s = w0 + off;
+      long long run = -1;  // (group, member) of this lane's entry, -1 none
+      long long cost = 0, light = 0;
+      int rep = -1;
+      if (s < P.nslots) {
+        const int k0 = k;
+        while (k + 1 < P.nlist && P.soff[P.list0 + k + 1] - P.slot0 <= s) ++k;
+        if (k != k0) i = -1;
+        const BigDesc d = P.desc[P.list0 + k];
+        const long long idx = s - (P.soff[P.list0 + k] - P.slot0);
+        if (d.base != nullptr && idx < d.E) {
+          const int ri = P.list[P.list0 + k];
+          const int gid = P.real[ri];
+          const int g = P.glen[gid];
+          const DeferredView V = Deferred(d.base, g);
+          if (i < 0 || idx >= V.eoff[i + 1] || idx < V.eoff[i]) {
+            int lo = 0, hi = g;  // last member with eoff <= idx
+            while (hi - lo > 1) {
+              const int mid = (lo + hi) >> 1;
+              if (V.eoff[mid] <= idx) lo = mid; else hi = mid;
+            }
+            i = lo;
+          }
+          rep = V.mq[i];
+          const int e0 = V.eoff[i];
+          const Entry e = Q.ent[Q.off[rep] + (idx - e0)];
+          const int t = EntNb(e);
+          const long long c = EntCnt(e);
+          const long long st = Q.size[t];
+          cost = EncodeCostForPair(rep, V.msz[i], t, st, c);
+          if (P.rc_before) {
+            if (HeavyEntry(V.msz[i], st, c)) {
+              const int rank = atomicAdd(&P.rc_nheavy[rep], 1);
+              if (rank < kHeavyMax) reinterpret_cast<int*>(&P.rc_heavy[rep])[rank] = static_cast<int>(idx - e0);
+            } else {
+              light = c;
+            }
+          }
+          const long long slot = P.soff[P.list0 + k] - P.slot0 + idx;
+          P.skey[slot] = (static_cast<unsigned long long>(k) << P.tbits) | static_cast<unsigned>(t);
+          P.sval[slot] = static_cast<unsigned long long>(i) << 32 | static_cast<unsigned long long>(c);
+          if (P.group_of[t] == gid) {
+            long long* pmat = reinterpret_cast<long long*>(P.mat + P.mat_off[ri]);
+            pmat[static_cast<long long>(i) * g + P.idx_in_group[t]] = c;
+          }
+          run = (static_cast<long long>(k) << 11) | i;
         }
       }
-      P.skey[slot + idx] = key_hi | static_cast<unsigned>(t);
-      P.sval[slot + idx] = static_cast<unsigned long long>(i) << 32 | static_cast<unsigned long long>(c);
-      if (P.group_of[t] == gid) pmat[static_cast<long long>(i) * g + P.idx_in_group[t]] = c;
-    }
-    // segmented inclusive scan over runs of equal member index
-    for (int o = 1; o < 32; o <<= 1) {
-      const long long vc = __shfl_up_sync(0xffffffffu, cost, o);
-      const long long vl = __shfl_up_sync(0xffffffffu, light, o);
-      const int vi = __shfl_up_sync(0xffffffffu, i, o);
-      if (lane >= o && vi == i) {
-        cost += vc;
-        light += vl;
+      // segmented inclusive scan over runs of equal (group, member)
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long vc = __shfl_up_sync(0xffffffffu, cost, o);
+        const long long vl = __shfl_up_sync(0xffffffffu, light, o);
+        const long long vr = __shfl_up_sync(0xffffffffu, run, o);
+        if (lane >= o && vr == run) {
+          cost += vc;
+          light += vl;
+        }
+      }
+      const long long next_run = __shfl_down_sync(0xffffffffu, run, 1);
+      if (run >= 0 && (lane == 31 || next_run != run)) {
+        const int ri = P.list[P.list0 + k];
+        const int g = P.glen[P.real[ri]];
+        unsigned long long* old_out =
+            reinterpret_cast<unsigned long long*>(P.mat + P.mat_off[ri] + OldCostOffset(static_cast<long long>(g) * g));
+        if (cost != 0) atomicAdd(&old_out[i], static_cast<unsigned long long>(cost));
+        if (P.rc_before) {
+          if (cost != 0) atomicAdd(reinterpret_cast<unsigned long long*>(&P.rc_before[rep]), static_cast<unsigned long long>(cost));
+          if (light != 0) atomicAdd(reinterpret_cast<unsigned long long*>(&P.rc_light[rep]), static_cast<unsigned long long>(light));
+        }
       }
     }
-    const int next_i = __shfl_down_sync(0xffffffffu, i, 1);
-    if (i >= 0 && (lane == 31 || next_i != i)) {
-      if (cost != 0) atomicAdd(&old_out[i], static_cast<unsigned long long>(cost));
-      if (P.rc_before) {
-        const int rep = V.mq[i];
-        if (cost != 0) atomicAdd(reinterpret_cast<unsigned long long*>(&P.rc_before[rep]), static_cast<unsigned long long>(cost));
-        if (light != 0) atomicAdd(reinterpret_cast<unsigned long long*>(&P.rc_light[rep]), static_cast<unsigned long long>(light));
-      }
-    }
+    __syncthreads();  // first_group is rewritten by the next window
   }
 }
 
@@ -1669,6 +1697,7 @@ struct ScoreParams {
   const unsigned char* keep;
   const float* zbuf;
   float* zpos;        // phase 1: logits of the exploration pairs passing the filter
+  long long* zgain;   // phase 1: their exact gains
   unsigned* npos;
   unsigned zcap;
   const float* cutoff;
@@ -1753,7 +1782,10 @@ __global__ void __launch_bounds__(kScoreThreads) ScoreKernel(ScoreParams P) {
         if (P.audit) atomicAdd(&P.stats[kStRkAuditPassing], 1ull);
         if (P.phase == 1) {
           const unsigned at = atomicAdd(P.npos, 1u);
-          if (at < P.zcap) P.zpos[at] = P.zbuf[slot];
+          if (at < P.zcap) {
+            P.zpos[at] = P.zbuf[slot];
+            P.zgain[at] = gain;
+          }
         }
       }
       P.res[slot] = make_longlong2(gain, before);
@@ -3241,7 +3273,10 @@ void Engine::SizeIterationBuffers(size_t R, size_t ncand, size_t nsel, size_t nb
     d_cand_feat_.ensure(ncand + 1);
     d_rk_keep_.ensure(ncand + 1);
     d_rk_zbuf_.ensure(ncand + 1);
-    for (int k = 0; k < 2; ++k) d_rk_zpos_[k].ensure(static_cast<size_t>(RankerExploreCap(static_cast<long long>(ncand))));
+    for (int k = 0; k < 2; ++k) {
+      d_rk_zpos_[k].ensure(static_cast<size_t>(RankerExploreCap(static_cast<long long>(ncand))));
+      d_rk_zgain_[k].ensure(static_cast<size_t>(RankerExploreCap(static_cast<long long>(ncand))));
+    }
   }
   rk_iter_slots_ = static_cast<long long>(ncand);
   d_sel_keep_.ensure(nsel + 1);
@@ -3462,15 +3497,12 @@ void Engine::LaunchPrepare(const BlockPlan& bp) {
     PP.sval = d_sval_[0].p;
     PP.skey_sorted = d_skey_[1].p;
     PP.sval_sorted = d_sval_[1].p;
-    // slices per deferred group: about 2048 row entries per CTA of the
-    // largest group (row totals as counted at Divide time)
-    const long long max_e = bp.max_e;
     ++launches_;
     PrepareKernel<<<b1 - b0, kPrepThreads, sizeof(PrepSmem), stream_>>>(PP);
     if (PP.nslots > 0) {
-      const unsigned slices = static_cast<unsigned>(std::min(512ll, std::max(1ll, (max_e + 2047) / 2048)));
+      const long long windows = (PP.nslots + kFillWindow - 1) / kFillWindow;
       ++launches_;
-      PrepareFillKernel<<<dim3(b1 - b0, slices), kFillThreads, 0, stream_>>>(PP);
+      PrepareFillKernel<<<static_cast<int>(std::min(windows, 152ll * 32)), kFillThreads, 0, stream_>>>(PP);
       // key = launch-local group index << tbits | target; the group index
       // stays below 2^(bits - tbits) - 1, so no key has the padding's low bits
       int bits = PP.tbits;
@@ -3524,6 +3556,7 @@ void Engine::RunBlock(const BlockPlan& bp, double threshold, int iter, int total
   SP.keep = d_rk_keep_.p;
   SP.zbuf = d_rk_zbuf_.p;
   SP.zpos = d_rk_zpos_[0].p;
+  SP.zgain = d_rk_zgain_[0].p;
   SP.npos = d_rk_npos_.p;
   SP.zcap = 0;
   SP.cutoff = d_rk_cut_.p;

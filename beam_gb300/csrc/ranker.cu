@@ -11,11 +11,14 @@
 // later iteration the ranker scores all candidates, a hashed exploration
 // subset (1/16) is scored exactly first, and the logit cutoff is the one that
 // keeps the requested recall of the subset's pairs passing the iteration's
-// threshold filter; candidates below it are not scored. Selection and commit
-// only ever see exactly scored pairs.
+// threshold filter, both of their number and of their exact gain (the merge
+// objective: a few high-gain pairs weigh more than many marginal ones);
+// candidates below it are not scored. Selection and commit only ever see
+// exactly scored pairs.
 #include <cuda_runtime.h>
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 #include <algorithm>
 #include <chrono>
@@ -325,20 +328,29 @@ __global__ void __launch_bounds__(kRkSlotThreads) RankerRankKernel(RkSlotParams 
   if ((threadIdx.x & 31) == 0 && ranked) atomicAdd(&P.stats[kStRkRanked], static_cast<unsigned long long>(ranked));
 }
 
-// Cutoff of the block from the sorted logits of the exploration pairs that
-// passed the threshold filter: the largest cutoff that keeps the requested
-// recall of them; too few of them: no pruning.
-__global__ void RankerCutoffKernel(const float* zpos_sorted, const unsigned* npos_p, unsigned cap, float recall,
-                                   float* cutoff) {
+// Cutoff of the block from the exploration pairs that passed the threshold
+// filter, sorted by logit with the inclusive prefix of their exact gains:
+// pairs with a logit below sorted[k] are pruned, with k the largest index such
+// that the pruned part holds at most (1 - recall) of the pairs AND at most
+// (1 - recall) of their total gain. Too few of them: no pruning.
+__global__ void RankerCutoffKernel(const float* zpos_sorted, const long long* gain_prefix, const unsigned* npos_p,
+                                   unsigned cap, float recall, float* cutoff) {
   const unsigned npos = min(*npos_p, cap);
   if (npos < 8) {
     *cutoff = -3.0e38f;
     return;
   }
-  const float miss = 1.0f - recall;
-  unsigned k = static_cast<unsigned>(floorf(miss * static_cast<float>(npos)));
+  const double miss = 1.0 - static_cast<double>(recall);
+  unsigned k = static_cast<unsigned>(floor(miss * static_cast<double>(npos)));
   if (k >= npos) k = npos - 1;
-  *cutoff = zpos_sorted[k];
+  // largest k' <= k with gain_prefix[k' - 1] <= miss * total (prefix of no pair = 0)
+  const double budget = miss * static_cast<double>(gain_prefix[npos - 1]);
+  unsigned lo = 0, hi = k;
+  while (lo < hi) {
+    const unsigned mid = (lo + hi + 1) >> 1;
+    if (static_cast<double>(gain_prefix[mid - 1]) <= budget) lo = mid; else hi = mid - 1;
+  }
+  *cutoff = zpos_sorted[lo];
 }
 
 // Logging iterations: a hashed sample of the block's scored slots with their
@@ -501,20 +513,28 @@ void Engine::RankerRank(int rg0, int nrg, long long slots, double threshold, int
   CheckCuda(cudaMemsetAsync(d_rk_npos_.p, 0, sizeof(unsigned), stream_), "memset npos");
   CheckCuda(cudaMemsetAsync(d_rk_zpos_[0].p, 0x7f, sizeof(float) * static_cast<size_t>(RankerExploreCap(slots)),
                             stream_), "memset zpos");
+  CheckCuda(cudaMemsetAsync(d_rk_zgain_[0].p, 0, sizeof(long long) * static_cast<size_t>(RankerExploreCap(slots)),
+                            stream_), "memset zgain");
 }
 
 long long Engine::RankerExploreCap(long long slots) const { return slots / 8 + 1024; }
 
 void Engine::RankerCutoff(long long slots) {
   const long long cap = RankerExploreCap(slots);
-  size_t bytes = 0;
-  CheckCuda(cub::DeviceRadixSort::SortKeys(nullptr, bytes, d_rk_zpos_[0].p, d_rk_zpos_[1].p, cap, 0, 32, stream_),
-            "cub sort size");
-  d_cub_tmp_.ensure(bytes);
-  CheckCuda(cub::DeviceRadixSort::SortKeys(d_cub_tmp_.p, bytes, d_rk_zpos_[0].p, d_rk_zpos_[1].p, cap, 0, 32,
-                                           stream_), "cub sort");
+  // logits ascending with their gains (the padding, above every logit with
+  // gain 0, sorts last), then the inclusive prefix of the gains
+  size_t sort_bytes = 0, scan_bytes = 0;
+  CheckCuda(cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, d_rk_zpos_[0].p, d_rk_zpos_[1].p, d_rk_zgain_[0].p,
+                                            d_rk_zgain_[1].p, cap, 0, 32, stream_), "cub sort size");
+  CheckCuda(cub::DeviceScan::InclusiveSum(nullptr, scan_bytes, d_rk_zgain_[1].p, d_rk_zgain_[0].p, cap, stream_),
+            "cub scan size");
+  d_cub_tmp_.ensure(std::max(sort_bytes, scan_bytes));
+  CheckCuda(cub::DeviceRadixSort::SortPairs(d_cub_tmp_.p, sort_bytes, d_rk_zpos_[0].p, d_rk_zpos_[1].p,
+                                            d_rk_zgain_[0].p, d_rk_zgain_[1].p, cap, 0, 32, stream_), "cub sort");
+  CheckCuda(cub::DeviceScan::InclusiveSum(d_cub_tmp_.p, scan_bytes, d_rk_zgain_[1].p, d_rk_zgain_[0].p, cap,
+                                          stream_), "cub scan");
   ++launches_;
-  RankerCutoffKernel<<<1, 1, 0, stream_>>>(d_rk_zpos_[1].p, d_rk_npos_.p, static_cast<unsigned>(cap),
+  RankerCutoffKernel<<<1, 1, 0, stream_>>>(d_rk_zpos_[1].p, d_rk_zgain_[0].p, d_rk_npos_.p, static_cast<unsigned>(cap),
                                            cfg_.ranker_recall, d_rk_cut_.p);
 }
 
