@@ -17,9 +17,9 @@ H2D copies, 20 iterations, partition download = D2H).
 The CPU side (cpu_baseline, and --impl reference) times the C oracle, a
 restatement of the reference path pinned to the reference's outputs, with
 OpenMP on all host cores (OMP_PROC_BIND=close, OMP_PLACES=cores), on bounded
-samples of the same workload: consecutive 64-group blocks of Merge, each
-sample charged its share of the iteration's Divide time. A full 20-iteration
-CPU run of this graph takes hours.
+samples of the same workload: 64-group blocks of Merge spread evenly over
+iteration 1, each charged its groups' share of the iteration's Divide time. A
+full 20-iteration CPU run of this graph takes hours.
 
 Multi-GPU (torchrun): replicas only - every rank runs the same workload on
 its own GPU with no collective on the data path.
@@ -489,55 +489,89 @@ def host_cpu() -> dict:
 
 
 def cpu_sample(g, steps: int, warmup: int, step_budget_s: float, threads: int) -> dict:
-    """The oracle on bounded samples of the workload: consecutive 64-group
-    blocks of Merge from iteration 1 on (a step = the blocks that start before
-    step_budget_s has run out, across iteration boundaries), each block charged
-    its groups' share of its iteration's Divide time."""
+    """The oracle on bounded samples of the workload: 64-group blocks of Merge
+    spread evenly over iteration 1 (every stride-th block from a few probe
+    blocks' timing, so that all steps end near the middle of the iteration
+    rather than all in its first groups), each block charged its groups' share
+    of the iteration's Divide time. A step is the blocks that start before
+    step_budget_s has run out. Blocks are sequentially dependent, so skipping
+    the ones between changes the state a little; the sample measures the cost
+    and the merges of representative blocks, not one exact run."""
     sys.path.insert(0, str(ROOT / "oracle"))
     from oracle import Oracle
 
     t0 = time.perf_counter()
     o = Oracle.from_graph(g, ea_use_threshold=True, threads=threads)
     setup_s = time.perf_counter() - t0
-    state = {"it": 1, "at": 0}
     t1 = time.perf_counter()
     o.divide(1)
-    state["divide_s"] = time.perf_counter() - t1
-    state["ngroups"] = o.group_count()
-    timed_merges, timed_s, timed_groups, iters = 0, 0.0, 0, set()
+    divide_s = time.perf_counter() - t1
+    ngroups = o.group_count()
+    bs = 64
+    nblocks = max(1, (ngroups + bs - 1) // bs)
+    accepted = lambda: o.stats()["accepted_merges_after_validation"]  # noqa: E731
+
+    def run_block(b: int) -> tuple[float, int, int]:
+        m0 = accepted()
+        t = time.perf_counter()
+        nxt = o.merge_blocks(1, b * bs, 1e-9)  # exactly one block
+        return time.perf_counter() - t, accepted() - m0, nxt - b * bs
+
+    # probe: the per-block cost of a few blocks spread over the iteration
+    probe = [run_block(b) for b in range(0, nblocks, max(1, nblocks // 16))][:16]
+    per_block = max(1e-6, sum(p[0] for p in probe) / len(probe))
+    if ITERATIONS * (nblocks * per_block + divide_s) <= 0.5 * (warmup + steps) * step_budget_s:
+        # a small graph: whole 20-iteration runs fit the budget, one per step
+        o.close()
+        timed_merges, timed_s, groups = 0, 0.0, 0
+        for step in range(warmup + steps):
+            o = Oracle.from_graph(g, ea_use_threshold=True, threads=threads)
+            t = time.perf_counter()
+            o.run(ITERATIONS)
+            dt = time.perf_counter() - t
+            if step >= warmup:
+                timed_merges += o.stats()["accepted_merges_after_validation"]
+                timed_s += dt
+            o.close()
+        return {"merges": timed_merges, "secs": timed_s, "groups": 0, "iterations": list(range(1, ITERATIONS + 1)),
+                "setup_s": setup_s, "stride": 0, "nblocks": nblocks, "full_runs": steps}
+    want = max(1, int((warmup + steps) * step_budget_s / per_block))
+    stride = max(1, nblocks // want)
+    order = list(range(stride // 2, nblocks, stride))
+    timed_merges, timed_s, timed_groups, pos = 0, 0.0, 0, 0
     for step in range(warmup + steps):
         merges, secs, groups = 0, 0.0, 0
         while secs < step_budget_s:
-            if state["at"] >= state["ngroups"]:
-                if state["it"] == ITERATIONS:
-                    # the whole run is done: a fresh run of the same graph goes on
-                    o.close()
-                    o = Oracle.from_graph(g, ea_use_threshold=True, threads=threads)
-                    state["it"] = 0
-                state["it"] += 1
-                state["at"] = 0
-                t3 = time.perf_counter()
-                o.divide(state["it"])
-                state["divide_s"] = time.perf_counter() - t3
-                state["ngroups"] = o.group_count()
-                continue
-            m0 = o.stats()["accepted_merges_after_validation"]
-            t2 = time.perf_counter()
-            nxt = o.merge_blocks(state["it"], state["at"], 1000.0 * (step_budget_s - secs))
-            dt = time.perf_counter() - t2
-            secs += dt + state["divide_s"] * (nxt - state["at"]) / max(1, state["ngroups"])
-            merges += o.stats()["accepted_merges_after_validation"] - m0
-            groups += nxt - state["at"]
-            if step >= warmup:
-                iters.add(state["it"])
-            state["at"] = nxt
+            if pos == len(order):
+                # a small graph runs out of blocks: the same blocks again, on a
+                # fresh partition (setup untimed, Divide timed again)
+                o.close()
+                o = Oracle.from_graph(g, ea_use_threshold=True, threads=threads)
+                t1 = time.perf_counter()
+                o.divide(1)
+                divide_s = time.perf_counter() - t1
+                pos = 0
+            dt, m, gcount = run_block(order[pos])
+            pos += 1
+            secs += dt + divide_s * gcount / max(1, ngroups)
+            merges += m
+            groups += gcount
         if step >= warmup:
             timed_merges += merges
             timed_s += secs
             timed_groups += groups
     o.close()
-    return {"merges": timed_merges, "secs": timed_s, "groups": timed_groups, "iterations": sorted(iters),
-            "setup_s": setup_s}
+    return {"merges": timed_merges, "secs": timed_s, "groups": timed_groups, "iterations": [1],
+            "setup_s": setup_s, "stride": stride, "nblocks": nblocks, "full_runs": 0}
+
+
+def sample_text(workload: str, r: dict) -> str:
+    head = f"the C oracle (the reference path restated, pinned to its outputs) on {workload}: "
+    if r["full_runs"]:
+        return head + f"whole 20-iteration runs ({r['merges']} merges, {r['secs']:.2f} s)"
+    return head + (f"every {r['stride']}th of the {r['nblocks']} 64-group blocks of iteration 1, {r['groups']} Divide "
+                   f"groups in all ({r['merges']} merges, {r['secs']:.2f} s including their share of Divide; oracle "
+                   f"setup {r['setup_s']:.1f} s untimed)")
 
 
 def reexec_with_omp_env() -> None:
@@ -574,10 +608,7 @@ def cpu_sample_main(args) -> None:
     print(json.dumps({
         "value": round(value, 1), "unit": UNIT, "cores": cpu["cores"], "kind": "port",
         "affinity": "OMP_PROC_BIND=close, OMP_PLACES=cores", "cpu_model": cpu["model"],
-        "sample": f"the C oracle (the reference path restated, pinned to its outputs) on {args.workload}: the first "
-                  f"{r['groups']} Divide groups of iteration(s) {r['iterations']} in 64-group blocks "
-                  f"({r['merges']} merges, {r['secs']:.2f} s including their share of Divide; oracle setup "
-                  f"{r['setup_s']:.1f} s untimed)"}), flush=True)
+        "sample": sample_text(args.workload, r)}), flush=True)
 
 
 def run_reference(args, dist: Dist) -> dict | None:
@@ -590,9 +621,7 @@ def run_reference(args, dist: Dist) -> dict | None:
     budget = args.reference_step_seconds
     r = cpu_sample(g, steps=args.steps, warmup=args.warmup, step_budget_s=budget, threads=cpu["cores"])
     value = r["merges"] / r["secs"] if r["secs"] > 0 else 0.0
-    sample = (f"consecutive 64-group blocks of Merge from iteration 1 on, about {budget:g} s per step "
-              f"({args.warmup} warm-up + {args.steps} timed steps, {r['groups']} Divide groups of iteration(s) "
-              f"{r['iterations']} timed, each step charged its groups' share of Divide)")
+    sample = sample_text(args.workload, r) + f"; {args.warmup} warm-up + {args.steps} timed steps of about {budget:g} s"
     return {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(1000.0 * r["secs"] / args.steps, 3), "higher_is_better": True,
