@@ -138,6 +138,9 @@ struct BlockCtl {
   unsigned int long_cnt;    // claimed neighbour rows rewritten by one CTA each
   unsigned int sel_total;   // selected pairs of the block (entries of the selection list)
   unsigned int pad;
+  // work queues of the dynamically scheduled kernels: the accumulate pass and
+  // the two scoring passes (exploration / the rest, or the only one)
+  unsigned long long work_next[3];
 };
 
 // One block of an iteration's plan: its real-group range, its candidate and
@@ -327,7 +330,9 @@ class Engine {
   DevBuf<long long> d_rc_before_, d_rc_light_;
   DevBuf<int4> d_rc_heavy_;
   DevBuf<int> d_rc_nheavy_;
-  bool plan_on_device_ = false;   // one-block iteration: Merge plans it on the device
+  bool plan_on_device_ = false;
+  int accum_grid_ = 152 * 4;  // resident CTAs of the dynamically scheduled kernels
+  int score_grid_ = 152 * 4;   // one-block iteration: Merge plans it on the device
   DevBuf<unsigned char> d_plan_tiles_;
   DevBuf<long long> d_plan_scalars_;
   PinnedBuf<long long> h_pin_;

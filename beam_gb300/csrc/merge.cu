@@ -912,17 +912,34 @@ __device__ __forceinline__ void AccumPair(const RunEntry& a, const RunEntry& b, 
 // chunks y + 1, y + 1 + kAccumSplit, ... of its run (warp 0 also within the
 // chunk), so a chunk deep in a long run is not one warp's long loop.
 constexpr int kAccumSplit = 4;
+// Work items are fetched from a queue, kAccumFetch at a time: a run over a
+// hub target makes some chunks far longer than others, so a static stride
+// leaves most warps idle behind a few. A fetch unit is one y of kAccumFetch
+// chunks spread over the whole slot range (chunk g, g + G, g + 2G, ... with G
+// fetch groups), so the consecutive chunks of one long run land on different
+// warps, and so do the split warps of one chunk.
+constexpr int kAccumFetch = 8;
 
 __global__ void __launch_bounds__(kAccumThreads) PrepareAccumKernel(PrepareParams P) {
   const int lane = threadIdx.x & 31;
   unsigned long long examined = 0;
   const long long nchunks = (P.nslots + 31) >> 5;
-  const long long nwork = nchunks * kAccumSplit;
-  const long long wstride = static_cast<long long>(gridDim.x) * (kAccumThreads / 32);
-  for (long long wk = (static_cast<long long>(blockIdx.x) * kAccumThreads + threadIdx.x) >> 5; wk < nwork;
-       wk += wstride) {
-    const long long ch = wk / kAccumSplit;
-    const int y = static_cast<int>(wk % kAccumSplit);
+  const long long ngroups8 = (nchunks + kAccumFetch - 1) / kAccumFetch;
+  const long long nfetch = ngroups8 * kAccumSplit;
+  long long fetched = -1, left = 0;
+  for (;;) {
+    if (left == 0) {
+      long long f = 0;
+      if (lane == 0) f = static_cast<long long>(atomicAdd(&P.ctl->work_next[0], 1ull));
+      fetched = __shfl_sync(0xffffffffu, f, 0);
+      if (fetched >= nfetch) break;
+      left = kAccumFetch;
+    }
+    --left;
+    // fetch unit u = (chunk group g, y): chunks g + k * ngroups8, k < kAccumFetch
+    const int y = static_cast<int>(fetched % kAccumSplit);
+    const long long ch = (fetched / kAccumSplit) + (kAccumFetch - 1 - left) * ngroups8;
+    if (ch >= nchunks) continue;
     const long long p0 = ch << 5;
     if (y > 0) {
       // nothing unless the chunk's first run reaches back at least y + 1 chunks
@@ -1680,6 +1697,7 @@ __global__ void __launch_bounds__(kSmallWarps * 32) PrepareSmallKernel(PreparePa
 
 struct ScoreParams {
   QuotientView Q;
+  BlockCtl* ctl;  // work queues of the scoring passes
   const int* order;
   const int* gstart;
   const int* real;
@@ -1740,17 +1758,40 @@ __device__ __forceinline__ void FlushScoreStats(unsigned long long* stats, const
 // One warp per candidate slot of the block (the concatenated per-group
 // candidate capacities); slots past a group's candidate count hold -1 and
 // are skipped.
+// Slots are fetched from the block's queue kScoreFetch at a time (pairs over
+// hub rows cost orders of magnitude more than the rest). Fetch c takes the
+// slots c, c + F, c + 2F, ... (F = the number of fetches): the candidates of
+// one member are consecutive slots, and a hub member's pairs must not all
+// land on one warp.
+constexpr int kScoreFetch = 16;
+
 __global__ void __launch_bounds__(kScoreThreads) ScoreKernel(ScoreParams P) {
   const long long s0 = P.cand_off[P.rg0];
   const long long s1 = P.cand_off[P.rg0 + P.nrg];
   const int lane = threadIdx.x & 31;
-  const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  const long long nw = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
   GainWork w = {0, 0, 0, 0, 0};
   long long pairs = 0, view_nnz = 0;
   unsigned long long pruned = 0;
   const float cutoff = P.phase == 2 ? *P.cutoff : 0.0f;
-  for (long long slot = s0 + warp; slot < s1; slot += nw) {
+  unsigned long long* queue = &P.ctl->work_next[P.phase == 2 ? 2 : 1];
+  const long long nfetch = (s1 - s0 + kScoreFetch - 1) / kScoreFetch;
+  long long slot = 0, left = 0;
+  for (;;) {
+    if (left == 0) {
+      long long f = 0;
+      if (lane == 0) f = static_cast<long long>(atomicAdd(queue, 1ull));
+      f = __shfl_sync(0xffffffffu, f, 0);
+      if (f >= nfetch) break;
+      slot = s0 + f;
+      left = kScoreFetch;
+    } else {
+      slot += nfetch;
+    }
+    --left;
+    if (slot >= s1) {
+      left = 0;
+      continue;
+    }
     const int2 ab = P.cand_rep[slot];
     if (ab.x < 0) continue;  // past the group's candidate count
     const int a = ab.x;
@@ -2823,6 +2864,9 @@ __global__ void __launch_bounds__(kRowsThreads) RewriteRowsKernel(CommitParams P
     P.ctl->short_cnt = 0;
     P.ctl->long_cnt = 0;
     P.ctl->sel_total = 0;
+    P.ctl->work_next[0] = 0;
+    P.ctl->work_next[1] = 0;
+    P.ctl->work_next[2] = 0;
     *P.ticket = 0u;
   }
 }
@@ -2856,6 +2900,14 @@ void Engine::ConfigureKernels() {
                                  static_cast<int>(sizeof(RowsSmem))), "commit smem attribute");
   CheckCuda(cudaFuncSetAttribute(RewriteRowsKernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(sizeof(RowsSmem))), "rewrite smem attribute");
+  // the queue-fed kernels launch exactly the CTAs that fit on the GPU at once
+  int sms = 0, per_sm = 0;
+  CheckCuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg_.device), "SM count");
+  CheckCuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, PrepareAccumKernel, kAccumThreads, 0),
+            "accumulate occupancy");
+  accum_grid_ = std::max(1, sms * per_sm);
+  CheckCuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ScoreKernel, kScoreThreads, 0), "score occupancy");
+  score_grid_ = std::max(1, sms * per_sm);
 }
 
 // Per-iteration layout: the groups with >= 2 members in Divide order, their
@@ -3426,7 +3478,10 @@ void Engine::LaunchCommit(int rg0, int nrg, int64_t max_pairs, bool verify) {
 // Row sums for the scoring pass: in a large block of a one-block iteration
 // (the prepare kernels write them while reading the member rows; scoring from
 // them pays in a large block).
-bool Engine::RowSumsOn(const BlockPlan& bp) const { return plans_.size() == 1 && bp.rg1 - bp.rg0 > kFewGroups; }
+// Row sums are written by the block's own prepare kernels from its block-start
+// state and read by its scoring pass only, so every block of more than
+// kFewGroups groups uses them, one-block iterations or not.
+bool Engine::RowSumsOn(const BlockPlan& bp) const { return bp.rg1 - bp.rg0 > kFewGroups; }
 
 void Engine::LaunchPrepare(const BlockPlan& bp) {
   const int s0 = bp.s0, s1 = bp.s1, b0 = bp.b0, b1 = bp.b1;
@@ -3515,7 +3570,7 @@ void Engine::LaunchPrepare(const BlockPlan& bp) {
                                                 d_sval_[1].p, PP.nslots, 0, bits, stream_), "cub radix sort");
       const long long want = ((PP.nslots + 31) / 32 * kAccumSplit + kAccumThreads / 32 - 1) / (kAccumThreads / 32);
       ++launches_;
-      PrepareAccumKernel<<<static_cast<int>(std::min(want, 152ll * 16)), kAccumThreads, 0, stream_>>>(PP);
+      PrepareAccumKernel<<<static_cast<int>(std::min<long long>(want, accum_grid_)), kAccumThreads, 0, stream_>>>(PP);
     }
     ++launches_;
     PrepareMembersKernel<<<static_cast<int>((members + 7) / 8), 256, 0, stream_>>>(PP);
@@ -3546,6 +3601,7 @@ void Engine::RunBlock(const BlockPlan& bp, double threshold, int iter, int total
   SP.cand = d_cand_.p;
   SP.cand_cnt = d_cand_cnt_.p;
   SP.cand_rep = d_cand_rep_.p;
+  SP.ctl = d_ctl_.p;
   SP.res = d_res_.p;
   SP.stats = d_stats_.p;
   SP.err = d_err_.p;
@@ -3565,7 +3621,8 @@ void Engine::RunBlock(const BlockPlan& bp, double threshold, int iter, int total
     // written by this block's prepare kernels
     SP.rc = RowConsts{d_rc_before_.p, d_rc_light_.p, d_rc_heavy_.p, d_rc_nheavy_.p};
   }
-  const int sgrid = static_cast<int>(std::min<long long>((slots + 7) / 8, 152 * 32));
+  const int sgrid = static_cast<int>(
+      std::min<long long>((slots + kScoreFetch * 8 - 1) / (kScoreFetch * 8), score_grid_));
   // learned ranker: trained after the logging iterations; afterwards the
   // exploration subset is scored first, then the rest above the cutoff
   const bool ranking = cfg_.ranker && rk_trained_ && iter > cfg_.ranker_train_iters;

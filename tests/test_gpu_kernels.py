@@ -186,6 +186,24 @@ def test_batched_form_matches_oracle(name):
     e.close()
 
 
+@pytest.mark.parametrize("name,batch", [("chunglu_twins", 300), ("chunglu_twins", 1000), ("rmat12", 257)])
+def test_multi_block_batched_form_matches_oracle(name, batch):
+    """Blocks of a few hundred to a thousand groups (several per iteration, each
+    scored from its own block-start row sums) against the oracle with the same
+    block size: the same partition and counters."""
+    from beam_gb300 import partition_hash
+    g, e, o = pair(SPECS[name], group_batch_size=batch)
+    e.run(20)
+    o.run(20)
+    assert partition_hash(e.partition()[0]) == o.partition_hash()
+    st, ost = e.stats(), o.stats()
+    for k in ("accepted_merges_after_validation", "merge_exact_gain_calls", "candidate_proxy_pairs_examined",
+              "update_touched_quotient_entries", "exact_union_neighbors", "exact_overlap_neighbors"):
+        assert st[k] == ost[k], k
+    assert st["blocks"] > 20
+    e.close()
+
+
 @pytest.mark.parametrize("batch", [64, 1 << 30])
 def test_validate_quotient_after_every_iteration(batch):
     """--validate-quotient: after every Merge the resident quotient graph equals
@@ -200,3 +218,17 @@ def test_validate_quotient_after_every_iteration(batch):
                 e.divide(it)
                 e.merge(it, 20)
                 e.validate_quotient()
+
+
+def test_block_size_tuner_picks_a_size_within_the_bound():
+    """beam_gb300.tune: the chosen block size keeps the cost ratio within the
+    bound of the plain form's, and is the fastest such size of the ladder."""
+    from beam_gb300 import Graph
+    from beam_gb300.tune import tune_block_size
+    g = Graph.generate(SPECS["chunglu_twins"])
+    r = tune_block_size(g, bound=0.001, ladder=(1 << 30, 1024, 256))
+    assert len(r["table"]) == 3
+    assert abs(r["delta_vs_plain"]) <= 0.001
+    ok = [t for t in r["table"] if t["within_bound"]]
+    if ok:
+        assert r["wall_s"] == min(t["wall_s"] for t in ok)
