@@ -160,8 +160,16 @@ __global__ void MarkNeedKernel(const int* __restrict__ order, const int* __restr
 // atomicMin; arcs are grouped by source, so this removes most atomics.
 __global__ void MinHashKernel(const int* __restrict__ arc_src, const int* __restrict__ col,
                               const int* __restrict__ label, const int* __restrict__ need, long long arcs, int n,
-                              int stamp, uint64_t base, unsigned long long* __restrict__ hash) {
+                              int stamp, uint64_t base, unsigned long long* __restrict__ hash,
+                              unsigned long long* __restrict__ stats) {
   const long long total = arcs + n;
+  // algorithmic bytes of one dimension: per arc its source, target, the
+  // source's label and its need stamp (16 B); per node its label and stamp
+  // and the supernode's hash word (16 B)
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    atomicAdd(&stats[kStDivideBytes], 16ull * static_cast<unsigned long long>(arcs) +
+                                          16ull * static_cast<unsigned long long>(n));
+  }
   const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
   for (long long t0 = static_cast<long long>(blockIdx.x) * blockDim.x; t0 < total; t0 += stride) {
     const long long t = t0 + threadIdx.x;
@@ -476,7 +484,7 @@ void Engine::Divide(int iter) {
         BeginTimed(kTimeDivide);
         ++launches_;
         MinHashKernel<<<152 * 8, 256, 0, s>>>(d_arc_src_.p, d_col_.p, d_label_.p, d_need_.p, arcs_, n,
-                                              need_stamp_, base, d_hash_.p);
+                                              need_stamp_, base, d_hash_.p, d_stats_.p);
         EndTimed(kTimeDivide);
       }
       ++launches_;

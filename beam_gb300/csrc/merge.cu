@@ -920,7 +920,7 @@ constexpr int kAccumSplit = 4;
 // warps, and so do the split warps of one chunk.
 constexpr int kAccumFetch = 8;
 
-__global__ void __launch_bounds__(kAccumThreads) PrepareAccumKernel(PrepareParams P) {
+__global__ void __launch_bounds__(kAccumThreads, 6) PrepareAccumKernel(PrepareParams P) {
   const int lane = threadIdx.x & 31;
   unsigned long long examined = 0;
   const long long nchunks = (P.nslots + 31) >> 5;
@@ -1352,8 +1352,9 @@ __global__ void __launch_bounds__(kPrepThreads) PrepareOutputKernel(PrepareParam
           const long long pg = pmat[static_cast<long long>(a) * g + b];
           long long denom = old[a] + old[b];
           if (denom < 1) denom = 1;
+          // a ranker feature, not a decision: single precision is enough
           P.cand_feat[P.cand_off[ri] + at] =
-              make_float2(static_cast<float>(pg), static_cast<float>(static_cast<double>(pg) / denom));
+              make_float2(static_cast<float>(pg), __fdividef(static_cast<float>(pg), static_cast<float>(denom)));
         }
         ++at;
       }
@@ -1676,7 +1677,7 @@ __global__ void __launch_bounds__(kSmallWarps * 32) PrepareSmallKernel(PreparePa
       const long long pg = S.p[TriIndex(lane, b, g)];
       long long denom = S.old[lane] + S.old[b];
       if (denom < 1) denom = 1;
-      feat[ex] = make_float2(static_cast<float>(pg), static_cast<float>(static_cast<double>(pg) / denom));
+      feat[ex] = make_float2(static_cast<float>(pg), __fdividef(static_cast<float>(pg), static_cast<float>(denom)));
     }
     P.cand_rep[P.cand_off[ri] + ex] = make_int2(S.q[lane], S.q[b]);
     out[ex++] = make_int2(lane, b);
@@ -1765,7 +1766,7 @@ __device__ __forceinline__ void FlushScoreStats(unsigned long long* stats, const
 // land on one warp.
 constexpr int kScoreFetch = 16;
 
-__global__ void __launch_bounds__(kScoreThreads) ScoreKernel(ScoreParams P) {
+__global__ void __launch_bounds__(kScoreThreads, 5) ScoreKernel(ScoreParams P) {
   const long long s0 = P.cand_off[P.rg0];
   const long long s1 = P.cand_off[P.rg0 + P.nrg];
   const int lane = threadIdx.x & 31;

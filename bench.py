@@ -170,6 +170,18 @@ KERNEL_OF_CLASS = {"score": "ScoreKernel", "prepare": "PrepareKernel", "update":
                    "divide": "MinHashKernel"}
 
 
+def union_roofline(t: dict, peak: float) -> dict:
+    """The scoring roofline with the reference's work counters: 8 B per row
+    entry of both rows, 4 B per union neighbour and 24 B per pair
+    (8 exact_gain_input_nnz + 4 exact_union_neighbors + 24 merge_exact_gain_calls)."""
+    u = t["union"]
+    nbytes = 8 * u["exact_gain_input_nnz"] + 4 * u["exact_union_neighbors"] + 24 * u["merge_exact_gain_calls"]
+    secs = t["kernel_ms"] / 1000.0
+    gbs = nbytes / secs / 1e9 if secs > 0 else 0.0
+    return {"algorithmic_bytes_per_launch": round(nbytes / max(1, t["kernel_launches"]), 1),
+            "achieved": round(gbs, 2), "frac": round(gbs / peak, 5) if peak else None}
+
+
 def profiled_traffic(kernel_class: str, workload: str, form: str) -> float | None:
     """Mean DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)
     from the committed ncu summary of this kernel on this workload and form."""
@@ -214,15 +226,21 @@ def form_engine(g, device: int, form: str):
     return Engine(g, device=device, ea_use_threshold=True, **FORMS[form])
 
 
-def kernel_breakdown(e) -> dict:
-    """Device time per kernel class over one untimed 20-iteration run each."""
+def kernel_breakdown(e, peak: float) -> dict:
+    """Device time per kernel class over one untimed 20-iteration run each,
+    with the class's algorithmic bytes (counted by its kernels) and the
+    roofline fraction they give against the HBM peak."""
     out = {}
     for name, kind in KERNEL_CLASSES.items():
         e.reset()
+        b0 = e.stats()[f"{name}_bytes"]
         e.set_timed_kernel(kind)
         e.run(ITERATIONS)
         ms, launches = e.timed_kernel()
-        out[name] = {"ms": round(ms, 3), "launches": launches}
+        nbytes = e.stats()[f"{name}_bytes"] - b0
+        gbs = nbytes / (ms / 1000.0) / 1e9 if ms > 0 else 0.0
+        out[name] = {"ms": round(ms, 3), "launches": launches, "algorithmic_bytes": nbytes,
+                     "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 5) if peak else None}
     e.set_timed_kernel(0)
     return out
 
@@ -231,6 +249,7 @@ def timed_steps(e, steps: int, dominant: str | None) -> dict:
     """steps x (reset, L2 flush, timed 20-iteration run); CUDA events on the
     engine stream around each run, the dominant kernel class timed inside."""
     step_ms, merges, kernel_ms, kernel_launches, kernel_bytes, step_launches = [], 0, 0.0, 0, 0, 0
+    union = {"exact_gain_input_nnz": 0, "exact_union_neighbors": 0, "merge_exact_gain_calls": 0}
     for _ in range(steps):
         e.reset()
         e.flush_l2()
@@ -248,11 +267,13 @@ def timed_steps(e, steps: int, dominant: str | None) -> dict:
             kernel_ms += ms
             kernel_launches += launches
             kernel_bytes += st1[f"{dominant}_bytes"] - st0[f"{dominant}_bytes"]
+            for k in ("exact_gain_input_nnz", "exact_union_neighbors", "merge_exact_gain_calls"):
+                union[k] += st1[k] - st0[k]
         merges += st1["accepted_merges_after_validation"] - st0["accepted_merges_after_validation"]
     e.synchronize()
     e.set_timed_kernel(0)
     return {"step_ms": step_ms, "merges": merges, "kernel_ms": kernel_ms, "kernel_launches": kernel_launches,
-            "kernel_bytes": kernel_bytes, "launches": step_launches}
+            "kernel_bytes": kernel_bytes, "launches": step_launches, "union": union}
 
 
 class PinnedGraph:
@@ -321,7 +342,8 @@ def run_ours(args, dist: Dist) -> dict | None:
     for _ in range(args.warmup):
         e.reset()
         e.run(ITERATIONS)
-    breakdown = kernel_breakdown(e)
+    peak, peak_kind = measured_peak()
+    breakdown = kernel_breakdown(e, peak)
     residency = hbm_residency(e, g)
     # the roofline kernel: ScoreKernel, the scoring kernel of the path
     dominant = args.timed_kernel or "score"
@@ -404,7 +426,6 @@ def run_ours(args, dist: Dist) -> dict | None:
     e2e_max = dist.reduce(sum(e2e_ms), "max")
     e2e_all = dist.reduce(float(e2e_merges), "sum")
 
-    peak, peak_kind = measured_peak()
     kernel_ms, kernel_launches = t["kernel_ms"], t["kernel_launches"]
     achieved = t["kernel_bytes"] / (kernel_ms / 1000.0) / 1e9 if kernel_ms > 0 else 0.0
     traffic = profiled_traffic(dominant, args.workload, head_form)
@@ -457,6 +478,9 @@ def run_ours(args, dist: Dist) -> dict | None:
             "peak_source": peak_kind,
             "traffic": traffic,
             "algorithmic_bytes_per_launch": round(t["kernel_bytes"] / max(1, kernel_launches), 1),
+            "bytes_counted": "8 B per row entry read, 4 B per shared-neighbour size, 36 B of row sums and 24 B "
+                             "per scored pair (the kernel's own reads)",
+            "union_count": union_roofline(t, peak),
             "avg_launch_us": round(1000.0 * kernel_ms / max(1, kernel_launches), 3),
             "launches": kernel_launches,
         },
@@ -664,7 +688,7 @@ def main():
     ap.add_argument("--workload", default="rmat24")
     ap.add_argument("--timed-kernel", choices=list(KERNEL_CLASSES), default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--form", choices=list(FORMS), default="batched",
+    ap.add_argument("--form", choices=list(FORMS), default="ranker",
                     help="form whose throughput is the headline value")
     ap.add_argument("--no-other-form", action="store_true", help="skip timing the other forms")
     ap.add_argument("--plain-steps", type=int, default=1, help="timed runs of the plain form")
