@@ -33,8 +33,8 @@ def test_reference_arm_json_line():
 def test_roofline_traffic_from_committed_summary():
     sys.path.insert(0, str(ROOT))
     import bench
-    traffic = bench.profiled_traffic("score", "rmat19", "batched")
-    text = (ROOT / "profiles" / "ScoreKernel_rmat19_batched_dram.md").read_text()
+    traffic = bench.profiled_traffic("score", "rmat24", "ranker")
+    text = (ROOT / "profiles" / "ScoreKernel_rmat24_ranker_dram.md").read_text()
     m = re.search(r"traffic_bytes_per_launch:\s*(\d+)", text)
     assert m and traffic == float(m.group(1)) and traffic > 0
 
