@@ -46,8 +46,16 @@ def gpu_metrics(case, tmp_path):
     return {k: str(v) for k, v in m.items()}, enc
 
 
+# the plain form at R-MAT scale 24 runs for about nine minutes on one GB300:
+# checked when BEAM_GPU_LONG=1 (the bench's plain run reports the same hash)
+LONG = {"rmat24"}
+
+
 @pytest.mark.parametrize("case", golden_cases(), ids=lambda c: c["name"])
 def test_gpu_matches_reference(case, tmp_path):
+    import os
+    if case["name"] in LONG and os.environ.get("BEAM_GPU_LONG") != "1":
+        pytest.skip("long case: set BEAM_GPU_LONG=1")
     got, enc = gpu_metrics(case, tmp_path)
     want = case["metrics"]
     diffs = {k: (want[k], got[k]) for k in got if k in want and want[k] != got[k]}
