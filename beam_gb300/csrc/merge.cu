@@ -59,7 +59,8 @@ constexpr int kSelectMidThreads = 128;
 constexpr int kSelectMidKeys = 512;   // >= min(C(32,2), 16 * 32) candidates
 constexpr int kRowsThreads = 256;
 constexpr int kRowSmem = 2048;       // staged row entries in shared memory
-constexpr int kWarpRow = 32;         // neighbour rows rewritten by one warp
+constexpr int kWarpRow = 32;         // neighbour rows rewritten by one warp in registers
+constexpr int kWarpRowMax = 256;     // neighbour rows rewritten by one warp through shared memory
 constexpr int kKeyIdxBits = 10;      // a_idx, b_idx < kMaxGroup
 constexpr long long kKeyGainMax = (1ll << (64 - 2 * kKeyIdxBits)) - 1;
 
@@ -2371,7 +2372,7 @@ struct CommitParams {
   BlockCtl* ctl;
   unsigned long long* stats;
   DevError* err;
-  int* rows_short;  // claimed neighbour rows of at most kWarpRow entries (count: ctl->short_cnt)
+  int* rows_short;  // claimed neighbour rows of at most kWarpRowMax entries (count: ctl->short_cnt)
   int* rows_long;   // the other claimed neighbour rows (count: ctl->long_cnt)
   unsigned* ticket; // last-CTA counter of the rewrite kernel, left at 0
   const int* sel_list;  // selection slots of the block's selected pairs (count: ctl->sel_total)
@@ -2416,6 +2417,8 @@ struct RowsSmem {
   int d[kRowSmem + 1];
   Entry ins[kRowSmem];
 };
+// every warp of a rewrite CTA has a kWarpRowMax slice of s and of ins
+static_assert(kWarpRowMax * (kRowsThreads / 32) <= kRowSmem, "warp slices of the rewrite buffers");
 
 // Rewrites a staged sorted row S[0..L) (adjacent equal ids allowed: the keep
 // row is staged as the merge of two rows) into out: duplicates are summed,
@@ -2591,7 +2594,7 @@ __global__ void __launch_bounds__(kRowsThreads) CommitKernel(CommitParams P) {
       if (sx == remove_stamp && P.seq[x] < my_seq && RowLookup(rr, lr, P.partner[x]) != 0) ++folded;
       if ((sx >> 1) == P.block_stamp) continue;  // keep/remove rows are rebuilt by their own pair
       if (atomicExch(&P.claim[x], P.block_stamp) != P.block_stamp) {
-        if (Q.len[x] <= kWarpRow) {
+        if (Q.len[x] <= kWarpRowMax) {
           P.rows_short[atomicAdd(&P.ctl->short_cnt, 1u)] = x;
         } else {
           P.rows_long[atomicAdd(&P.ctl->long_cnt, 1u)] = x;
@@ -2687,7 +2690,7 @@ __global__ void __launch_bounds__(256) CommitShortKernel(CommitParams P) {
         const int sx = P.stamp[x];
         if (sx == remove_stamp && P.seq[x] < my_seq && RowLookup(rr, lr, P.partner[x]) != 0) folded = 1;
         if ((sx >> 1) != P.block_stamp && atomicExch(&P.claim[x], P.block_stamp) != P.block_stamp) {
-          if (Q.len[x] <= kWarpRow) {
+          if (Q.len[x] <= kWarpRowMax) {
             P.rows_short[atomicAdd(&P.ctl->short_cnt, 1u)] = x;
           } else {
             P.rows_long[atomicAdd(&P.ctl->long_cnt, 1u)] = x;
@@ -2765,13 +2768,122 @@ __global__ void __launch_bounds__(256) CommitShortKernel(CommitParams P) {
   }
 }
 
-// Claimed neighbour rows of at most kWarpRow entries, one warp per row: each
-// entry of a supernode removed in this block is renamed to its keep partner,
-// the row is sorted by neighbour (register bitonic sort), equal neighbours
-// are summed and the row is compacted in place (it can only shrink).
-__device__ void RewriteShortRows(const CommitParams& P) {
+// A claimed neighbour row of kWarpRow < L <= kWarpRowMax entries, one warp,
+// staged in the warp's slice S of shared memory. Only the entries of
+// supernodes removed in this block change: each is renamed to its keep
+// partner and summed into the partner's entry when the row has one, else
+// inserted (INS, sorted). Every other entry keeps its order, so its new
+// position is its old one less the renamed entries before it plus the
+// inserted entries below it: no sort of the row. Returns the new length.
+__device__ int RewriteMediumRow(const CommitParams& P, Entry* row, int L, Entry* S, Entry* INS) {
+  constexpr int kChunks = kWarpRowMax / 32;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const int remove_stamp = 2 * P.block_stamp + 1;
+  for (int j = lane; j < L; j += 32) S[j] = row[j];
+  __syncwarp();
+  unsigned rm[kChunks];  // renamed entries of each 32-entry chunk (warp-uniform)
+  int m = 0;             // inserted entries so far
+#pragma unroll
+  for (int t = 0; t < kChunks; ++t) {
+    const int j = lane + 32 * t;
+    bool renamed = false, insert = false;
+    Entry ins = 0;
+    if (j < L) {
+      const Entry e = S[j];
+      const int id = EntNb(e);
+      if (P.stamp[id] == remove_stamp) {
+        renamed = true;
+        const int kp = P.partner[id];
+        const long long c = EntCnt(e);
+        int lo = 0, hi = L;  // kp among the staged ids (only counts change meanwhile)
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (EntNb(S[mid]) < kp) lo = mid + 1; else hi = mid;
+        }
+        if (lo < L && EntNb(S[lo]) == kp) {
+          atomicAdd(reinterpret_cast<unsigned long long*>(&S[lo]), static_cast<unsigned long long>(c));
+        } else {
+          insert = true;
+          ins = MakeEnt(kp, c);
+        }
+      }
+    }
+    rm[t] = __ballot_sync(0xffffffffu, renamed);
+    const unsigned im = __ballot_sync(0xffffffffu, insert);
+    if (insert) INS[m + __popc(im & lt)] = ins;
+    m += __popc(im);
+  }
+  // the inserted entries in id order (distinct ids: one remove per keep)
+  int pow2 = 1;
+  while (pow2 < m) pow2 <<= 1;
+  for (int i = m + lane; i < pow2; i += 32) INS[i] = ~0ull;
+  __syncwarp();
+  for (int k = 2; k <= pow2; k <<= 1) {
+    for (int jj = k >> 1; jj > 0; jj >>= 1) {
+      for (int i = lane; i < pow2; i += 32) {
+        const int ixj = i ^ jj;
+        if (ixj > i) {
+          const Entry a = INS[i];
+          const Entry b = INS[ixj];
+          if ((a > b) == ((i & k) == 0)) {
+            INS[i] = b;
+            INS[ixj] = a;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+  // renamed entries before position q of the staged row
+  auto dropped_before = [&](int q) {
+    int d = 0;
+#pragma unroll
+    for (int t = 0; t < kChunks; ++t) {
+      if (32 * t + 32 <= q) d += __popc(rm[t]);
+      else if (32 * t < q) d += __popc(rm[t] & ((1u << (q - 32 * t)) - 1u));
+    }
+    return d;
+  };
+  int k_total = 0;
+#pragma unroll
+  for (int t = 0; t < kChunks; ++t) k_total += __popc(rm[t]);
+#pragma unroll
+  for (int t = 0; t < kChunks; ++t) {
+    const int j = lane + 32 * t;
+    if (j < L && !((rm[t] >> lane) & 1u)) {
+      const Entry e = S[j];
+      int lo = 0, hi = m;  // inserted entries below this id
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (EntNb(INS[mid]) < EntNb(e)) lo = mid + 1; else hi = mid;
+      }
+      row[j - dropped_before(j) + lo] = e;
+    }
+  }
+  for (int i = lane; i < m; i += 32) {
+    const Entry e = INS[i];
+    int lo = 0, hi = L;  // staged entries below the inserted id
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (EntNb(S[mid]) < EntNb(e)) lo = mid + 1; else hi = mid;
+    }
+    row[lo - dropped_before(lo) + i] = e;
+  }
+  __syncwarp();
+  return L - k_total + m;
+}
+
+// Claimed neighbour rows of at most kWarpRowMax entries, one warp per row.
+// Rows of at most kWarpRow entries: each entry of a supernode removed in this
+// block is renamed to its keep partner, the row is sorted by neighbour
+// (register bitonic sort), equal neighbours are summed and the row is
+// compacted in place (it can only shrink). Longer ones: RewriteMediumRow with
+// the warp's slice of the CTA's shared memory.
+__device__ void RewriteShortRows(const CommitParams& P, RowsSmem& R) {
   const QuotientView& Q = P.Q;
   const int lane = threadIdx.x & 31;
+  const int warp_in_cta = threadIdx.x >> 5;
   const unsigned cnt = P.ctl->short_cnt;
   const int remove_stamp = 2 * P.block_stamp + 1;
   const long long nw = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
@@ -2780,6 +2892,16 @@ __device__ void RewriteShortRows(const CommitParams& P) {
     const int x = P.rows_short[idx];
     Entry* row = Q.ent + Q.off[x];
     const int lx = Q.len[x];
+    if (lx > kWarpRow) {
+      const int nl = RewriteMediumRow(P, row, lx, R.s + warp_in_cta * kWarpRowMax, R.ins + warp_in_cta * kWarpRowMax);
+      if (lane == 0) {
+        Q.len[x] = nl;
+        ++rows;
+        entries += static_cast<unsigned long long>(lx);
+        bytes += 8ull * static_cast<unsigned long long>(lx + nl);
+      }
+      continue;
+    }
     unsigned long long key = ~0ull;
     if (lane < lx) {
       const Entry e = row[lane];
@@ -2853,7 +2975,8 @@ __global__ void __launch_bounds__(kRowsThreads) RewriteRowsKernel(CommitParams P
   RowsSmem& R = *reinterpret_cast<RowsSmem*>(smem_raw);
   __shared__ bool last;
   RewriteLongRows(P, R);
-  RewriteShortRows(P);
+  __syncthreads();  // the shared buffers pass from the CTA's long rows to its warps
+  RewriteShortRows(P, R);
   // the last CTA to finish clears the block control words for the next
   // block (every CTA has read them and made its scratch allocations by now)
   __threadfence();
