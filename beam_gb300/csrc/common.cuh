@@ -147,11 +147,8 @@ __device__ __forceinline__ long long WarpSum(long long v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
-__device__ __forceinline__ int WarpSumInt(int v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
+// one redux.sync instead of five shuffles (the same two's-complement sum)
+__device__ __forceinline__ int WarpSumInt(int v) { return __reduce_add_sync(0xffffffffu, v); }
 __device__ __forceinline__ long long WarpMax(long long v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {

@@ -155,13 +155,23 @@ __global__ void MarkNeedKernel(const int* __restrict__ order, const int* __restr
   }
 }
 
-// One thread per arc (plus one per node for the node's own rank). Lanes of a
+// One lane per arc (plus one per node for the node's own rank). Lanes of a
 // warp whose sources share a supernode combine their minima before a single
 // atomicMin; arcs are grouped by source, so this removes most atomics.
-__global__ void MinHashKernel(const int* __restrict__ arc_src, const int* __restrict__ col,
-                              const int* __restrict__ label, const int* __restrict__ need, long long arcs, int n,
-                              int stamp, uint64_t base, unsigned long long* __restrict__ hash,
-                              unsigned long long* __restrict__ stats) {
+// Each warp takes kHashUnroll consecutive 32-item steps at a time and issues
+// each level of the dependent chain (source, its label, the label's need
+// stamp, the target) for all of them before the next level, so a lane keeps
+// kHashUnroll loads in flight instead of one: the pass is bound by that
+// chain's latency, not by its bytes. Steps whose lanes need nothing (most of
+// them past depth 0, where only the oversized segments are hashed) skip the
+// warp reduction.
+constexpr int kHashUnroll = 4;
+
+__global__ void __launch_bounds__(256) MinHashKernel(const int* __restrict__ arc_src, const int* __restrict__ col,
+                                                     const int* __restrict__ label, const int* __restrict__ need,
+                                                     long long arcs, int n, int stamp, uint64_t base,
+                                                     unsigned long long* __restrict__ hash,
+                                                     unsigned long long* __restrict__ stats) {
   const long long total = arcs + n;
   // algorithmic bytes of one dimension: per arc its source, target, the
   // source's label and its need stamp (16 B); per node its label and stamp
@@ -170,30 +180,44 @@ __global__ void MinHashKernel(const int* __restrict__ arc_src, const int* __rest
     atomicAdd(&stats[kStDivideBytes], 16ull * static_cast<unsigned long long>(arcs) +
                                           16ull * static_cast<unsigned long long>(n));
   }
-  const long long stride = static_cast<long long>(gridDim.x) * blockDim.x;
-  for (long long t0 = static_cast<long long>(blockIdx.x) * blockDim.x; t0 < total; t0 += stride) {
-    const long long t = t0 + threadIdx.x;
-    int rep = -1;
-    unsigned long long h = ~0ull;
-    if (t < total) {
-      const int node = t < arcs ? arc_src[t] : static_cast<int>(t - arcs);
-      const int r = label[node];
-      if (need[r] == stamp) {
-        rep = r;
-        h = HashRankWithBase(base, t < arcs ? col[t] : node);
-      }
+  const int lane = threadIdx.x & 31;
+  const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
+  constexpr long long kTile = 32ll * kHashUnroll;
+  for (long long t0 = warp * kTile; t0 < total; t0 += nwarps * kTile) {
+    int node[kHashUnroll], rep[kHashUnroll];
+#pragma unroll
+    for (int u = 0; u < kHashUnroll; ++u) {
+      const long long t = t0 + 32 * u + lane;
+      node[u] = t < arcs ? arc_src[t] : t < total ? static_cast<int>(t - arcs) : -1;
     }
-    // exact minimum over the lanes holding the same supernode: high words
-    // first, then low words among the lanes that hold the minimal high word
-    const unsigned mask = __match_any_sync(0xffffffffu, rep);
-    const unsigned hi = static_cast<unsigned>(h >> 32);
-    const unsigned lo = static_cast<unsigned>(h & 0xffffffffu);
-    const unsigned mhi = __reduce_min_sync(mask, hi);
-    const unsigned mlo = __reduce_min_sync(mask, hi == mhi ? lo : 0xffffffffu);
-    const unsigned long long g = (static_cast<unsigned long long>(mhi) << 32) | mlo;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(mask) - 1;
-    if (rep >= 0 && lane == leader) atomicMin(&hash[rep], g);
+#pragma unroll
+    for (int u = 0; u < kHashUnroll; ++u) rep[u] = node[u] >= 0 ? label[node[u]] : -1;
+#pragma unroll
+    for (int u = 0; u < kHashUnroll; ++u) {
+      if (rep[u] >= 0 && need[rep[u]] != stamp) rep[u] = -1;
+    }
+    int x[kHashUnroll];
+#pragma unroll
+    for (int u = 0; u < kHashUnroll; ++u) {
+      const long long t = t0 + 32 * u + lane;
+      x[u] = rep[u] < 0 ? 0 : t < arcs ? col[t] : node[u];
+    }
+#pragma unroll
+    for (int u = 0; u < kHashUnroll; ++u) {
+      if (__ballot_sync(0xffffffffu, rep[u] >= 0) == 0u) continue;
+      const unsigned long long h = rep[u] >= 0 ? HashRankWithBase(base, x[u]) : ~0ull;
+      // exact minimum over the lanes holding the same supernode: high words
+      // first, then low words among the lanes that hold the minimal high word
+      const unsigned mask = __match_any_sync(0xffffffffu, rep[u]);
+      const unsigned hi = static_cast<unsigned>(h >> 32);
+      const unsigned lo = static_cast<unsigned>(h & 0xffffffffu);
+      const unsigned mhi = __reduce_min_sync(mask, hi);
+      const unsigned mlo = __reduce_min_sync(mask, hi == mhi ? lo : 0xffffffffu);
+      const unsigned long long g = (static_cast<unsigned long long>(mhi) << 32) | mlo;
+      const int leader = __ffs(mask) - 1;
+      if (rep[u] >= 0 && lane == leader) atomicMin(&hash[rep[u]], g);
+    }
   }
 }
 

@@ -228,6 +228,24 @@ __device__ __forceinline__ void RecordHeavy(int4* slot, int& nh, bool heavy, int
 constexpr int kProbeMinLong = 256;
 constexpr int kProbeRatio = 8;
 
+// The last index i of [lo, hi) with a[i] <= x, for a non-decreasing array
+// with a[lo] <= x, found by the whole warp (warp-uniform arguments): each
+// round probes 32 points of the remaining span, so the search takes about
+// log32 of the span in dependent loads instead of log2.
+__device__ __forceinline__ int WarpLastLE(const long long* __restrict__ a, int lo, int hi, long long x) {
+  const int lane = threadIdx.x & 31;
+  while (hi - lo > 1) {
+    // lo < p, p <= hi - 1, non-decreasing over the lanes
+    const int p = lo + 1 + static_cast<int>((static_cast<long long>(hi - lo - 1) * lane) >> 5);
+    const int k = __popc(__ballot_sync(0xffffffffu, a[p] <= x));  // lanes 0..k-1 hold
+    const int p_lo = __shfl_sync(0xffffffffu, p, k > 0 ? k - 1 : 0);
+    const int p_hi = __shfl_sync(0xffffffffu, p, k < 32 ? k : 31);
+    if (k > 0) lo = p_lo;
+    if (k < 32) hi = p_hi;
+  }
+  return lo;
+}
+
 // First position of a sorted row whose neighbour is >= x.
 __device__ __forceinline__ int RowLowerBound(const Entry* row, int len, int x) {
   int lo = 0, hi = len;
@@ -247,24 +265,48 @@ __device__ __forceinline__ int RowLowerBound(const Entry* row, int len, int x) {
 // neighbours need sizes and cost terms; the tiled merge that finds them is
 // the one of WarpExactGain. The same integers as the full merge, term by
 // term regrouped.
-__device__ void WarpExactGainShared(const QuotientView& Q, const RowConsts& RC, int a, int b, long long* gain_out,
-                                    long long* before_out, GainWork* work, DevError* err) {
+// The scalars of one row that the row-sum gain reads: staged in shared memory
+// by the scoring warp for a whole fetch of pairs at once (independent loads,
+// one latency for all of them), then read by every lane as broadcasts.
+struct RowMeta {
+  long long off, internal, before, light;
+  int4 heavy;
+  int len, size, nheavy;
+  int rep;  // the row's supernode
+};
+
+__device__ __forceinline__ void LoadRowMeta(const QuotientView& Q, const RowConsts& RC, int r, RowMeta* m) {
+  RowMeta v;
+  v.off = Q.off[r];
+  v.internal = Q.internal[r];
+  v.before = RC.before[r];
+  v.light = RC.light[r];
+  v.heavy = RC.heavy[r];
+  v.len = Q.len[r];
+  v.size = Q.size[r];
+  v.nheavy = RC.nheavy[r];
+  v.rep = r;
+  *m = v;
+}
+
+__device__ void WarpExactGainShared(const QuotientView& Q, int a, int b, const RowMeta& A, const RowMeta& B,
+                                    long long* gain_out, long long* before_out, GainWork* work, DevError* err) {
   constexpr unsigned kFull = 0xffffffffu;
   constexpr Entry kPadEntry = static_cast<Entry>(0x7fffffffull) << 32;
-  const int ha = RC.nheavy[a];
-  const int hb = RC.nheavy[b];
+  const int ha = A.nheavy;
+  const int hb = B.nheavy;
   if (ha > kHeavyMax || hb > kHeavyMax) {
     WarpExactGain(Q, a, b, gain_out, before_out, work, err);
     return;
   }
   const int lane = threadIdx.x & 31;
-  const long long sa = Q.size[a];
-  const long long sb = Q.size[b];
+  const long long sa = A.size;
+  const long long sb = B.size;
   const long long sw = sa + sb;
-  const Entry* ra = Q.ent + Q.off[a];
-  const Entry* rb = Q.ent + Q.off[b];
-  const int la = Q.len[a];
-  const int lb = Q.len[b];
+  const Entry* ra = Q.ent + A.off;
+  const Entry* rb = Q.ent + B.off;
+  const int la = A.len;
+  const int lb = B.len;
   long long shared = 0, eab_a = 0, eab_b = 0;
   int ovl = 0, bad = 0;
   const bool a_long = la >= lb;
@@ -352,7 +394,7 @@ __device__ void WarpExactGainShared(const QuotientView& Q, const RowConsts& RC, 
     const bool on_a = lane < kHeavyMax;
     const int h = on_a ? lane : lane - kHeavyMax;
     if (h < (on_a ? ha : hb)) {
-      const int4 hp = on_a ? RC.heavy[a] : RC.heavy[b];
+      const int4 hp = on_a ? A.heavy : B.heavy;
       const int pos = h == 0 ? hp.x : h == 1 ? hp.y : h == 2 ? hp.z : hp.w;
       const Entry e = (on_a ? ra : rb)[pos];
       const long long term = BlockCost(sw, Q.size[EntNb(e)], EntCnt(e), false, bad);
@@ -368,11 +410,11 @@ __device__ void WarpExactGainShared(const QuotientView& Q, const RowConsts& RC, 
   if (eab_a != eab_b) {
     if (lane == 0) RaiseError(err, kErrAsymmetric, a, b, 0);
   }
-  const long long ia = Q.internal[a];
-  const long long ib = Q.internal[b];
-  const long long before = RC.before[a] + RC.before[b] - BlockCost(sb, sa, eab_b, false, bad) +
+  const long long ia = A.internal;
+  const long long ib = B.internal;
+  const long long before = A.before + B.before - BlockCost(sb, sa, eab_b, false, bad) +
                            BlockCost(sa, sa, ia, true, bad) + BlockCost(sb, sb, ib, true, bad);
-  const long long after = RC.light[a] + RC.light[b] - BlockCost(sw, sb, eab_a, false, bad) -
+  const long long after = A.light + B.light - BlockCost(sw, sb, eab_a, false, bad) -
                           BlockCost(sw, sa, eab_b, false, bad) + shared +
                           BlockCost(sw, sw, ia + ib + eab_a, true, bad);
   if (bad && lane == 0) RaiseError(err, kErrBlockCost, a, b, 0);
@@ -970,11 +1012,20 @@ __global__ void __launch_bounds__(kAccumThreads, 6) PrepareAccumKernel(PreparePa
       me.q = r.q;
       st = P.Q.size[t];
     }
-    // pairs inside the chunk
+    // pairs inside the chunk: each lane visits the earlier lanes holding its
+    // key, one per round (a chunk whose targets are all distinct, the common
+    // case, takes no round)
     if (y == 0) {
-      for (int src = 0; src < 31; ++src) {
+      unsigned earlier = __match_any_sync(0xffffffffu, me.key) & ((1u << lane) - 1u);
+      if (!valid) earlier = 0u;
+      const int rounds = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(__popc(earlier))));
+      for (int r = 0; r < rounds; ++r) {
+        const int src = earlier != 0u ? __ffs(earlier) - 1 : lane;
         const RunEntry o = ShflRunEntry(me, src);
-        if (valid && src < lane && o.key == me.key) AccumPair(me, o, t, st, g, pmat, examined);
+        if (earlier != 0u) {
+          AccumPair(me, o, t, st, g, pmat, examined);
+          earlier &= earlier - 1u;
+        }
       }
     }
     // the run holding the chunk's first slot may start in earlier chunks
@@ -1039,7 +1090,19 @@ __device__ __forceinline__ void MembersTopK(int lane, int g, int i, int qi, int 
   }
   float cut = 0.0f;
   if (cnt > top_k + 16) {
-    unsigned lo = 0, hi = 0x7f800000u;  // count(bits >= lo) >= top_k > count(bits >= hi)
+    // count(bits >= lo) >= top_k > count(bits >= hi), starting from the
+    // smallest and one past the largest positive ratio (the cnt candidates)
+    unsigned lo = 0x7f800000u, hi = 0;
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const unsigned b = __float_as_uint(rf[t]);
+      if (rf[t] > 0.0f) {
+        lo = b < lo ? b : lo;
+        hi = b > hi ? b : hi;
+      }
+    }
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi) + 1u;
     while (hi - lo > 1) {
       const unsigned mid = lo + ((hi - lo) >> 1);
       int c = 0;
@@ -1166,11 +1229,7 @@ __global__ void __launch_bounds__(256) PrepareMembersKernel(PrepareParams P) {
   const long long total = P.moff[P.list0 + P.nlist] - P.moff[P.list0];
   if (wg >= total) return;
   const long long target = P.moff[P.list0] + wg;
-  int lo = P.list0, hi = P.list0 + P.nlist;  // last entry with moff <= target
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (P.moff[mid] <= target) lo = mid; else hi = mid;
-  }
+  const int lo = WarpLastLE(P.moff, P.list0, P.list0 + P.nlist, target);  // last entry with moff <= target
   const int ri = P.list[lo];
   const int i = static_cast<int>(target - P.moff[lo]);
   const int gid = P.real[ri];
@@ -1729,10 +1788,11 @@ struct ScoreParams {
   DevError* err;
 };
 
-__device__ __forceinline__ void ScoreGain(const ScoreParams& P, int a, int b, long long* gain, long long* before,
-                                          GainWork* w) {
+// m: the two rows' staged scalars (read only with row sums)
+__device__ __forceinline__ void ScoreGain(const ScoreParams& P, int a, int b, const RowMeta* m, long long* gain,
+                                          long long* before, GainWork* w) {
   if (P.rc.before) {
-    WarpExactGainShared(P.Q, P.rc, a, b, gain, before, w, P.err);
+    WarpExactGainShared(P.Q, a, b, m[0], m[1], gain, before, w, P.err);
   } else {
     WarpExactGain(P.Q, a, b, gain, before, w, P.err);
   }
@@ -1764,77 +1824,112 @@ __device__ __forceinline__ void FlushScoreStats(unsigned long long* stats, const
 // hub rows cost orders of magnitude more than the rest). Fetch c takes the
 // slots c, c + F, c + 2F, ... (F = the number of fetches): the candidates of
 // one member are consecutive slots, and a hub member's pairs must not all
-// land on one warp.
+// land on one warp. The warp loads the fetch's pair ids and (with row sums)
+// the scalars of their rows together, one slot or row per lane, before it
+// scores the pairs one by one: one load latency per fetch instead of a chain
+// of them per pair.
 constexpr int kScoreFetch = 16;
+static_assert(2 * kScoreFetch == 32, "one staged row per lane");
 
-__global__ void __launch_bounds__(kScoreThreads, 5) ScoreKernel(ScoreParams P) {
+__global__ void __launch_bounds__(kScoreThreads, 4) ScoreKernel(ScoreParams P) {
+  __shared__ RowMeta s_meta[kScoreThreads / 32][2 * kScoreFetch];
+  constexpr unsigned kFull = 0xffffffffu;
   const long long s0 = P.cand_off[P.rg0];
   const long long s1 = P.cand_off[P.rg0 + P.nrg];
   const int lane = threadIdx.x & 31;
+  RowMeta* wm = s_meta[threadIdx.x >> 5];
   GainWork w = {0, 0, 0, 0, 0};
   long long pairs = 0, view_nnz = 0;
   unsigned long long pruned = 0;
   const float cutoff = P.phase == 2 ? *P.cutoff : 0.0f;
   unsigned long long* queue = &P.ctl->work_next[P.phase == 2 ? 2 : 1];
   const long long nfetch = (s1 - s0 + kScoreFetch - 1) / kScoreFetch;
-  long long slot = 0, left = 0;
   for (;;) {
-    if (left == 0) {
-      long long f = 0;
-      if (lane == 0) f = static_cast<long long>(atomicAdd(queue, 1ull));
-      f = __shfl_sync(0xffffffffu, f, 0);
-      if (f >= nfetch) break;
-      slot = s0 + f;
-      left = kScoreFetch;
-    } else {
-      slot += nfetch;
+    long long f = 0;
+    if (lane == 0) f = static_cast<long long>(atomicAdd(queue, 1ull));
+    f = __shfl_sync(kFull, f, 0);
+    if (f >= nfetch) break;
+    // lane j < kScoreFetch: slot j of the fetch, its pair, and what to do
+    // with it (0 nothing, 1 score, 2 pruned by the ranker)
+    const long long slot = s0 + f + static_cast<long long>(lane & (kScoreFetch - 1)) * nfetch;
+    int2 ab = make_int2(-1, -1);
+    int todo = 0;
+    if (lane < kScoreFetch && slot < s1) {
+      ab = P.cand_rep[slot];
+      if (ab.x >= 0) {
+        todo = 1;
+        if (P.phase == 1 && P.keep[slot] != 1) todo = 0;  // phase 1 scores the exploration slots
+        if (P.phase == 2) {
+          if (P.keep[slot] == 1) {
+            todo = 0;  // exploration slot, scored in phase 1
+          } else if (P.zbuf[slot] < cutoff) {
+            todo = 2;
+          }
+        }
+      }
     }
-    --left;
-    if (slot >= s1) {
-      left = 0;
-      continue;
+    // lane l stages row (l & 1) of pair l >> 1: its supernode and, with row
+    // sums, its scalars
+    {
+      const int j = lane >> 1;
+      const int ja = __shfl_sync(kFull, ab.x, j);
+      const int jb = __shfl_sync(kFull, ab.y, j);
+      const int jt = __shfl_sync(kFull, todo, j);
+      const int r = (lane & 1) ? jb : ja;
+      if (P.rc.before && (jt == 1 || (jt == 2 && P.audit))) {
+        LoadRowMeta(P.Q, P.rc, r, &wm[lane]);
+      } else {
+        wm[lane].rep = r;
+      }
     }
-    const int2 ab = P.cand_rep[slot];
-    if (ab.x < 0) continue;  // past the group's candidate count
-    const int a = ab.x;
-    const int b = ab.y;
-    long long gain = 0, before = 0;
-    if (P.phase == 1 && P.keep[slot] != 1) continue;
-    if (P.phase == 2) {
-      if (P.keep[slot] == 1) continue;  // exploration slot, scored in phase 1
-      if (P.zbuf[slot] < cutoff) {
+    const unsigned prune = __ballot_sync(kFull, todo == 2);
+    unsigned live = __ballot_sync(kFull, todo != 0);
+    __syncwarp();
+    for (; live != 0u; live &= live - 1u) {
+      const int j = __ffs(live) - 1;
+      const RowMeta* m = wm + 2 * j;
+      const int a = m[0].rep;
+      const int b = m[1].rep;
+      const long long sj = s0 + f + static_cast<long long>(j) * nfetch;
+      long long gain = 0, before = 0;
+      if ((prune >> j) & 1u) {
         // pruned by the ranker: not scored (the audit scores it aside)
         if (P.audit) {
           GainWork aw = {0, 0, 0, 0, 0};
-          ScoreGain(P, a, b, &gain, &before, &aw);
+          ScoreGain(P, a, b, m, &gain, &before, &aw);
           if (lane == 0 && PassesFilter(gain, before, P.threshold, P.use_threshold)) {
             atomicAdd(&P.stats[kStRkAuditPassing], 1ull);
             atomicAdd(&P.stats[kStRkAuditLost], 1ull);
           }
         }
         if (lane == 0) {
-          P.res[slot] = make_longlong2(0, -1);
+          P.res[sj] = make_longlong2(0, -1);
           ++pruned;
         }
         continue;
       }
-    }
-    ScoreGain(P, a, b, &gain, &before, &w);
-    if (lane == 0) {
-      if (P.phase != 0 && PassesFilter(gain, before, P.threshold, P.use_threshold)) {
-        if (P.audit) atomicAdd(&P.stats[kStRkAuditPassing], 1ull);
-        if (P.phase == 1) {
-          const unsigned at = atomicAdd(P.npos, 1u);
-          if (at < P.zcap) {
-            P.zpos[at] = P.zbuf[slot];
-            P.zgain[at] = gain;
+      ScoreGain(P, a, b, m, &gain, &before, &w);
+      if (lane == 0) {
+        if (P.phase != 0 && PassesFilter(gain, before, P.threshold, P.use_threshold)) {
+          if (P.audit) atomicAdd(&P.stats[kStRkAuditPassing], 1ull);
+          if (P.phase == 1) {
+            const unsigned at = atomicAdd(P.npos, 1u);
+            if (at < P.zcap) {
+              P.zpos[at] = P.zbuf[sj];
+              P.zgain[at] = gain;
+            }
           }
         }
+        P.res[sj] = make_longlong2(gain, before);
+        ++pairs;
+        if (P.rc.before) {
+          view_nnz += m[0].len + (m[0].internal > 0 ? 1 : 0) + m[1].len + (m[1].internal > 0 ? 1 : 0);
+        } else {
+          view_nnz += P.Q.len[a] + (P.Q.internal[a] > 0 ? 1 : 0) + P.Q.len[b] + (P.Q.internal[b] > 0 ? 1 : 0);
+        }
       }
-      P.res[slot] = make_longlong2(gain, before);
-      ++pairs;
-      view_nnz += P.Q.len[a] + (P.Q.internal[a] > 0 ? 1 : 0) + P.Q.len[b] + (P.Q.internal[b] > 0 ? 1 : 0);
     }
+    __syncwarp();  // the next fetch restages this warp's rows
   }
   if (lane == 0) {
     FlushScoreStats(P.stats, w, pairs, view_nnz);
