@@ -287,46 +287,78 @@ __global__ void MixedRunsKernel(const unsigned long long* __restrict__ keys, con
   }
 }
 
-// Second pass, one CTA: each recorded run is reordered stably by its keys
-// (the items of the smallest remaining key move first, in their order) via
-// the scratch arrays; the run counter is cleared for the next sort.
-__global__ void SortMixedRunsKernel(unsigned long long* __restrict__ keys, int* __restrict__ vals,
-                                    const int* __restrict__ item_seg, const int* __restrict__ uend,
-                                    const int* __restrict__ list, int* __restrict__ cnt,
-                                    unsigned long long* __restrict__ tk, int* __restrict__ tv) {
+// Second pass, a warp per recorded run: the run is reordered stably by its
+// keys (the items of the smallest remaining key move first, in their order)
+// via the scratch arrays. A run shares its high word, so each round takes the
+// smallest remaining low word by one warp reduction and moves its items by a
+// ballot compaction; a long run (a large segment of one min-hash colliding
+// with another) is read 32 items at a time instead of by one thread.
+__global__ void __launch_bounds__(256) SortMixedRunsKernel(unsigned long long* __restrict__ keys,
+                                                           int* __restrict__ vals, const int* __restrict__ item_seg,
+                                                           const int* __restrict__ uend, const int* __restrict__ list,
+                                                           const int* __restrict__ cnt,
+                                                           unsigned long long* __restrict__ tk, int* __restrict__ tv) {
+  constexpr unsigned kFull = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
   const int nruns = *cnt;
-  for (int t = threadIdx.x; t < nruns; t += blockDim.x) {
+  const int nwarps = static_cast<int>((static_cast<long long>(gridDim.x) * blockDim.x) >> 5);
+  for (int t = static_cast<int>((static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5); t < nruns;
+       t += nwarps) {
     const int r0 = list[t];
-    const unsigned long long hi = keys[r0] >> 32;
+    const unsigned hi = static_cast<unsigned>(keys[r0] >> 32);
     const int e = uend[item_seg[r0]];
-    int r1 = r0 + 1;
-    while (r1 < e && (keys[r1] >> 32) == hi) ++r1;
-    int w = r0;
-    unsigned long long last = 0;
-    bool any = false;
-    while (w < r1) {
-      unsigned long long mn = ~0ull;
-      for (int i = r0; i < r1; ++i) {
-        const unsigned long long k = keys[i];
-        if ((!any || k > last) && k < mn) mn = k;
+    int r1 = r0 + 1;  // one past the run: the first later item of another high word
+    for (;;) {
+      const int i = r1 + lane;
+      const unsigned in = __ballot_sync(kFull, i < e && static_cast<unsigned>(keys[i] >> 32) == hi);
+      if (in != kFull) {
+        r1 += __ffs(~in) - 1;
+        break;
       }
-      for (int i = r0; i < r1; ++i) {
-        if (keys[i] == mn) {
-          tk[w] = mn;
-          tv[w] = vals[i];
-          ++w;
+      r1 += 32;
+    }
+    int w = r0;
+    unsigned last = 0;
+    bool any = false;  // a low word has been moved (last is valid)
+    while (w < r1) {
+      unsigned mn = 0xffffffffu;
+      bool have = false;
+      for (int i = r0 + lane; i < r1; i += 32) {
+        const unsigned lo = static_cast<unsigned>(keys[i]);
+        if ((!any || lo > last) && lo <= mn) {
+          mn = lo;
+          have = true;
         }
+      }
+      mn = __reduce_min_sync(kFull, have ? mn : 0xffffffffu);
+      if (__ballot_sync(kFull, have) == 0u) break;  // every item moved
+      for (int i0 = r0; i0 < r1; i0 += 32) {
+        const int i = i0 + lane;
+        unsigned long long k = 0;
+        bool hit = false;
+        if (i < r1) {
+          k = keys[i];
+          hit = static_cast<unsigned>(k) == mn && (!any || mn > last);
+        }
+        const unsigned m = __ballot_sync(kFull, hit);
+        if (hit) {
+          const int at = w + __popc(m & lt);
+          tk[at] = k;
+          tv[at] = vals[i];
+        }
+        w += __popc(m);
       }
       last = mn;
       any = true;
     }
-    for (int i = r0; i < r1; ++i) {
+    __syncwarp();
+    for (int i = r0 + lane; i < r1; i += 32) {
       keys[i] = tk[i];
       vals[i] = tv[i];
     }
+    __syncwarp();
   }
-  __syncthreads();
-  if (threadIdx.x == 0) *cnt = 0;
 }
 
 __global__ void ScatterSortedKernel(const int* __restrict__ pos_map, const int* __restrict__ item_seg,
@@ -390,7 +422,7 @@ void Engine::Divide(int iter) {
   int* uend = ubeg + n;
   int* seg_start = d_seg_beg_.p;
   int* item_seg = d_seg_end_.p;
-  int* fix_cnt = uend + n + 8;  // mixed-run counter (cleared by each second pass)
+  int* fix_cnt = uend + n + 8;  // mixed-run counter (cleared before each first pass)
   d_fix_list_.ensure(static_cast<size_t>(n) + 1);
   d_keys_hi_[0].ensure(static_cast<size_t>(n) + 1);
   d_unf_pk_[0].ensure(static_cast<size_t>(n) + 1);
@@ -546,10 +578,11 @@ void Engine::Divide(int iter) {
       // runs of equal high words with mixed low words into full-key order
       // (d_keys_ / d_vals_ are free once gathered)
       ++launches_;
+      CheckCuda(cudaMemsetAsync(fix_cnt, 0, sizeof(int), s), "memset mixed-run counter");
       MixedRunsKernel<<<Blocks(items, T), T, 0, s>>>(d_keys_alt_.p, item_seg, ubeg, items, d_fix_list_.p, fix_cnt);
       ++launches_;
-      SortMixedRunsKernel<<<1, T, 0, s>>>(d_keys_alt_.p, d_vals_alt_.p, item_seg, uend, d_fix_list_.p, fix_cnt,
-                                          d_keys_.p, d_vals_.p);
+      SortMixedRunsKernel<<<152 * 2, 256, 0, s>>>(d_keys_alt_.p, d_vals_alt_.p, item_seg, uend, d_fix_list_.p,
+                                                  fix_cnt, d_keys_.p, d_vals_.p);
       ++launches_;
       ScatterSortedKernel<<<Blocks(items, T), T, 0, s>>>(d_pos_map_.p, item_seg, ubeg, items, d_keys_alt_.p,
                                                          d_vals_alt_.p, fallback ? 1 : 0, cfg_.divide_max_group,
