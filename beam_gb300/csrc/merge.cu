@@ -32,6 +32,7 @@
 #include <cub/device/device_radix_sort.cuh>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "engine.h"
@@ -520,8 +521,12 @@ struct PrepareParams {
 __host__ __device__ __forceinline__ long long FlagOffset(long long gg) { return 8 * gg; }
 __host__ __device__ __forceinline__ long long OldCostOffset(long long gg) { return (9 * gg + 7) & ~7ll; }
 
+// rb: the bits of the candidate's double ratio (the reference's rounded
+// quotient, computed once per candidate); positive doubles order like their
+// bit patterns, so candidates are compared on the integer pipes (this GPU's
+// FP64 rate is a small fraction of its integer rate)
 struct RankKey {
-  double ratio;
+  unsigned long long rb;
   long long pg;
   int lo, hi, j;
 };
@@ -529,10 +534,42 @@ struct RankKey {
 // ranked_better (src/sweg.cpp:1926-1938): ratio desc, proxy gain desc,
 // rep_lo asc, rep_hi asc.
 __device__ __forceinline__ bool Better(const RankKey& x, const RankKey& y) {
-  if (x.ratio != y.ratio) return x.ratio > y.ratio;
+  if (x.rb != y.rb) return x.rb > y.rb;
   if (x.pg != y.pg) return x.pg > y.pg;
   if (x.lo != y.lo) return x.lo < y.lo;
   return x.hi < y.hi;
+}
+
+// The reference's threshold test RN(gain / before) >= threshold (doubles, gain
+// and before > 0) on the integer pipes, with threshold = m * 2^-e exactly
+// (split on the host; e < 0: no split). Rounding is monotonic, so a quotient
+// at or above the threshold passes, and one more than 2^-51 (relative) below
+// it rounds below it and fails; only the band in between, and counts of 2^53
+// or more (which the double conversion rounds), take the double division.
+struct ThresholdBits {
+  unsigned long long m;
+  int e;
+};
+
+__host__ inline ThresholdBits SplitThreshold(double threshold) {
+  ThresholdBits t{0, -1};
+  if (threshold > 0.0 && std::isfinite(threshold)) {
+    int ex = 0;
+    const double f = std::frexp(threshold, &ex);  // threshold = f * 2^ex, f in [0.5, 1)
+    t.m = static_cast<unsigned long long>(std::ldexp(f, 53));
+    t.e = 53 - ex;
+  }
+  return t;
+}
+
+__device__ __forceinline__ bool RatioAtLeast(long long gain, long long before, double threshold, ThresholdBits t) {
+  if (t.e >= 0 && t.e <= 63 && gain < (1ll << 53) && before < (1ll << 53)) {
+    const unsigned __int128 l = static_cast<unsigned __int128>(static_cast<unsigned long long>(gain)) << t.e;
+    const unsigned __int128 r = static_cast<unsigned __int128>(t.m) * static_cast<unsigned long long>(before);
+    if (l >= r) return true;
+    if (l + (r >> 51) < r) return false;
+  }
+  return static_cast<double>(gain) / static_cast<double>(before) >= threshold;
 }
 
 __device__ __forceinline__ unsigned BucketHash(int t, unsigned mask) {
@@ -1065,7 +1102,8 @@ __device__ __forceinline__ void MembersTopK(int lane, int g, int i, int qi, int 
   auto ratio_of = [&](int j, long long pg) {
     long long denom = old_i + old[j];
     if (denom < 1) denom = 1;
-    return static_cast<double>(pg) / static_cast<double>(denom);
+    return static_cast<unsigned long long>(
+        __double_as_longlong(static_cast<double>(pg) / static_cast<double>(denom)));
   };
   // fp32 prescreen: the exact (double) ratio is only computed for the
   // candidates that can be in the member's top_k. The fp32 ratio of a
@@ -1132,7 +1170,7 @@ __device__ __forceinline__ void MembersTopK(int lane, int g, int i, int qi, int 
     __syncwarp();
     const bool have = lane < npass;
     RankKey mine;
-    mine.ratio = 0.0;
+    mine.rb = 0;
     mine.pg = 0;
     mine.lo = 0;
     mine.hi = 0;
@@ -1142,7 +1180,7 @@ __device__ __forceinline__ void MembersTopK(int lane, int g, int i, int qi, int 
       const long long pg = prow[j];
       const int qj = q[j];
       mine.j = j;
-      mine.ratio = ratio_of(j, pg);
+      mine.rb = ratio_of(j, pg);
       mine.pg = pg;
       mine.lo = qi < qj ? qi : qj;
       mine.hi = qi < qj ? qj : qi;
@@ -1150,7 +1188,7 @@ __device__ __forceinline__ void MembersTopK(int lane, int g, int i, int qi, int 
     int rank = 0;
     for (int o = 0; o < npass; ++o) {
       RankKey other;
-      other.ratio = __shfl_sync(0xffffffffu, mine.ratio, o);
+      other.rb = __shfl_sync(0xffffffffu, mine.rb, o);
       other.pg = __shfl_sync(0xffffffffu, mine.pg, o);
       other.lo = __shfl_sync(0xffffffffu, mine.lo, o);
       other.hi = __shfl_sync(0xffffffffu, mine.hi, o);
@@ -1173,7 +1211,7 @@ __device__ __forceinline__ void MembersTopK(int lane, int g, int i, int qi, int 
       const long long pg = prow[j];
       RankKey k;
       k.j = j;
-      k.ratio = ratio_of(j, pg);
+      k.rb = ratio_of(j, pg);
       k.pg = pg;
       const int qj = q[j];
       k.lo = qi < qj ? qi : qj;
@@ -1195,7 +1233,7 @@ __device__ __forceinline__ void MembersTopK(int lane, int g, int i, int qi, int 
       int src = lane;
       for (int o = 16; o > 0; o >>= 1) {
         RankKey other;
-        other.ratio = __shfl_xor_sync(0xffffffffu, best.ratio, o);
+        other.rb = __shfl_xor_sync(0xffffffffu, best.rb, o);
         other.pg = __shfl_xor_sync(0xffffffffu, best.pg, o);
         other.lo = __shfl_xor_sync(0xffffffffu, best.lo, o);
         other.hi = __shfl_xor_sync(0xffffffffu, best.hi, o);
@@ -1249,7 +1287,8 @@ __global__ void __launch_bounds__(256) PrepareMembersKernel(PrepareParams P) {
   auto ratio_of = [&](int j, long long pg) {
     long long denom = old_i + old[j];
     if (denom < 1) denom = 1;
-    return static_cast<double>(pg) / static_cast<double>(denom);
+    return static_cast<unsigned long long>(
+        __double_as_longlong(static_cast<double>(pg) / static_cast<double>(denom)));
   };
   int cnt = 0;
   for (int base = 0; base < g; base += 32) {
@@ -1291,7 +1330,7 @@ __global__ void __launch_bounds__(256) PrepareMembersKernel(PrepareParams P) {
         if (pg <= 0) continue;
         RankKey k;
         k.j = j;
-        k.ratio = ratio_of(j, pg);
+        k.rb = ratio_of(j, pg);
         k.pg = pg;
         const int qj = q[j];
         k.lo = qi < qj ? qi : qj;
@@ -1304,7 +1343,7 @@ __global__ void __launch_bounds__(256) PrepareMembersKernel(PrepareParams P) {
       }
       for (int o = 16; o > 0; o >>= 1) {
         RankKey other;
-        other.ratio = __shfl_xor_sync(0xffffffffu, best.ratio, o);
+        other.rb = __shfl_xor_sync(0xffffffffu, best.rb, o);
         other.pg = __shfl_xor_sync(0xffffffffu, best.pg, o);
         other.lo = __shfl_xor_sync(0xffffffffu, best.lo, o);
         other.hi = __shfl_xor_sync(0xffffffffu, best.hi, o);
@@ -1782,6 +1821,7 @@ struct ScoreParams {
   const float* cutoff;
   int audit;          // phase 2: score pruned slots aside and count the ones the filter passes
   double threshold;
+  ThresholdBits thr;  // threshold split for the integer test
   int use_threshold;
   RowConsts rc;  // row sums of the block-start state (rc.before == nullptr: full merge)
   unsigned long long* stats;
@@ -1798,10 +1838,11 @@ __device__ __forceinline__ void ScoreGain(const ScoreParams& P, int a, int b, co
   }
 }
 
-__device__ __forceinline__ bool PassesFilter(long long gain, long long before, double threshold, int use_threshold) {
+__device__ __forceinline__ bool PassesFilter(long long gain, long long before, double threshold, ThresholdBits thr,
+                                             int use_threshold) {
   if (gain <= 0) return false;
   if (!use_threshold) return true;
-  return before > 0 && static_cast<double>(gain) / static_cast<double>(before) >= threshold;
+  return before > 0 && RatioAtLeast(gain, before, threshold, thr);
 }
 
 __device__ __forceinline__ void FlushScoreStats(unsigned long long* stats, const GainWork& w, long long pairs,
@@ -1897,7 +1938,7 @@ __global__ void __launch_bounds__(kScoreThreads, 4) ScoreKernel(ScoreParams P) {
         if (P.audit) {
           GainWork aw = {0, 0, 0, 0, 0};
           ScoreGain(P, a, b, m, &gain, &before, &aw);
-          if (lane == 0 && PassesFilter(gain, before, P.threshold, P.use_threshold)) {
+          if (lane == 0 && PassesFilter(gain, before, P.threshold, P.thr, P.use_threshold)) {
             atomicAdd(&P.stats[kStRkAuditPassing], 1ull);
             atomicAdd(&P.stats[kStRkAuditLost], 1ull);
           }
@@ -1910,7 +1951,7 @@ __global__ void __launch_bounds__(kScoreThreads, 4) ScoreKernel(ScoreParams P) {
       }
       ScoreGain(P, a, b, m, &gain, &before, &w);
       if (lane == 0) {
-        if (P.phase != 0 && PassesFilter(gain, before, P.threshold, P.use_threshold)) {
+        if (P.phase != 0 && PassesFilter(gain, before, P.threshold, P.thr, P.use_threshold)) {
           if (P.audit) atomicAdd(&P.stats[kStRkAuditPassing], 1ull);
           if (P.phase == 1) {
             const unsigned at = atomicAdd(P.npos, 1u);
@@ -1983,6 +2024,7 @@ struct SelectParams {
   int* seq;
   int block_stamp;
   double threshold;
+  ThresholdBits thr;  // threshold split for the integer test
   int use_threshold;
   unsigned char* scratch;
   unsigned long long scratch_cap;
@@ -2071,8 +2113,7 @@ __global__ void __launch_bounds__(kThreads) SelectKernel(SelectParams P) {
         ++my_rej;
         continue;
       }
-      const double ratio = static_cast<double>(gain) / static_cast<double>(before);
-      if (ratio < P.threshold) {
+      if (!RatioAtLeast(gain, before, P.threshold, P.thr)) {
         ++my_rej;
         continue;
       }
@@ -2196,7 +2237,7 @@ __device__ __forceinline__ void SelectMatchGroup(const SelectParams& P, int ri) 
     if (before < 0) continue;  // pruned by the ranker before scoring
     bool ok = gain > 0;
     if (ok && P.use_threshold) {
-      ok = before > 0 && static_cast<double>(gain) / static_cast<double>(before) >= P.threshold;
+      ok = before > 0 && RatioAtLeast(gain, before, P.threshold, P.thr);
     }
     if (!ok) {
       ++my_rej;
@@ -2359,7 +2400,7 @@ __global__ void __launch_bounds__(kSelectSmallWarps * 32) SelectSmallKernel(Sele
       if (before >= 0) {  // negative: pruned by the ranker before scoring
         bool ok = gain > 0;
         if (ok && P.use_threshold) {
-          ok = before > 0 && static_cast<double>(gain) / static_cast<double>(before) >= P.threshold;
+          ok = before > 0 && RatioAtLeast(gain, before, P.threshold, P.thr);
         }
         if (!ok) {
           rej = 1;
@@ -3825,6 +3866,7 @@ void Engine::RunBlock(const BlockPlan& bp, double threshold, int iter, int total
   SP.stats = d_stats_.p;
   SP.err = d_err_.p;
   SP.threshold = threshold;
+  SP.thr = SplitThreshold(threshold);
   SP.use_threshold = cfg_.ea_use_threshold ? 1 : 0;
   SP.audit = cfg_.ranker_audit ? 1 : 0;
   SP.phase = 0;
@@ -3884,6 +3926,7 @@ void Engine::RunBlock(const BlockPlan& bp, double threshold, int iter, int total
   LP.seq = d_seq_.p;
   LP.block_stamp = block_stamp_;
   LP.threshold = threshold;
+  LP.thr = SplitThreshold(threshold);
   LP.use_threshold = cfg_.ea_use_threshold ? 1 : 0;
   LP.scratch = d_scratch_.p;
   LP.scratch_cap = d_scratch_.n;

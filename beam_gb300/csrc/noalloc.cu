@@ -374,6 +374,15 @@ int beam_prepare_flat_noalloc(const int32_t* offsets, const int32_t* row_rep_ids
     return Fail("null device pointer");
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  {
+    // the call reads its status back and waits for the stream: not a graph node
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    const cudaError_t cst = cudaStreamIsCapturing(s, &cap);
+    if (cst != cudaSuccess) return Fail(std::string("cudaStreamIsCapturing: ") + cudaGetErrorString(cst));
+    if (cap != cudaStreamCaptureStatusNone) {
+      return Fail("the stream is capturing: the call waits for its stream and cannot be captured in a CUDA graph");
+    }
+  }
   if (rows < 2) {
     cudaError_t st = cudaMemsetAsync(out_count, 0, sizeof(int32_t), s);
     if (st == cudaSuccess) st = cudaStreamSynchronize(s);

@@ -234,8 +234,9 @@ const char* beam_engine_last_error(void);
  * array of about 3 MB, resident on every GPU that loads the library until the
  * process exits, shared by all calls: its contents stay from the last call
  * (the kernel clears what must start at zero) and calls that overlap on the
- * GPU race. The first call on each device looks up the array's device
- * address; make that first call before any stream capture. */
+ * GPU race. The call reads its status back and waits for its stream, so it
+ * cannot be captured in a CUDA graph: on a capturing stream it fails with a
+ * message and enqueues nothing. */
 int beam_prepare_flat_noalloc(const int32_t* offsets, const int32_t* row_rep_ids, const int32_t* neighbors,
                               const int64_t* weights, const int64_t* neighbor_sizes, const int64_t* row_sizes,
                               const int64_t* row_internal, int32_t rows, int64_t num_entries, int32_t top_k,

@@ -231,3 +231,39 @@ def test_noalloc_reports_bad_inputs():
     if want is not None:
         assert np.array_equal(got, want)
     o.close()
+
+
+def test_noalloc_refuses_stream_capture():
+    """On a capturing stream the call fails with a message and enqueues
+    nothing (it reads its status back and waits for its stream); the capture
+    stays valid, and a call after it succeeds."""
+    import torch
+    from beam_gb300 import _native as N
+    _, o = oracle_after_first_merge()
+    order, starts, lengths = o.groups()
+    s, ln = max(zip(starts.tolist(), lengths.tolist()), key=lambda x: x[1])
+    q = order[s:s + min(ln, 64)].copy()
+    f = flat_group(oracle_rows(o), q)
+    dev = {k: torch.from_numpy(v.copy()).cuda() for k, v in f.items()}
+    g = len(f["reps"])
+    cap = min(g * (g - 1) // 2, g * 16)
+    out_a = torch.zeros(cap, dtype=torch.int32, device="cuda")
+    out_b = torch.zeros(cap, dtype=torch.int32, device="cuda")
+    out_n = torch.full((1,), -7, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    stream = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=stream):
+        rc = N.lib().beam_prepare_flat_noalloc(
+            dev["offsets"].data_ptr(), dev["reps"].data_ptr(), dev["nb"].data_ptr(), dev["wt"].data_ptr(),
+            dev["nbsz"].data_ptr(), dev["rsz"].data_ptr(), dev["rint"].data_ptr(), g, len(f["nb"]), 16,
+            out_a.data_ptr(), out_b.data_ptr(), cap, out_n.data_ptr(), C.c_void_p(stream.cuda_stream))
+        out_n.fill_(5)
+    msg = N.lib().beam_prepare_flat_noalloc_last_error().decode()
+    assert rc != 0 and "cannot be captured" in msg
+    graph.replay()
+    torch.cuda.synchronize()
+    assert int(out_n.item()) == 5
+    rc, pairs, n, msg = call_raw(f)
+    assert rc == 0 and n == len(pairs) and n > 0
+    o.close()
