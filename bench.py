@@ -14,6 +14,13 @@ timed beside it for the speed-ups and the cost-ratio comparison. e2e runs the
 public C ABI from pinned host buffers every step (create from the host CSR =
 H2D copies, 20 iterations, partition download = D2H).
 
+The whole run keeps to a wall budget (--time-budget-s, 23 minutes by
+default). The plain form runs last, in a child process stopped when the
+budget is spent: at this scale one plain run is about 9 minutes of
+latency-bound 64-group blocks, and a form that cannot finish is reported
+as incomplete instead of holding the GPU past the budget. The CPU baseline's
+child is bounded the same way.
+
 The CPU side (cpu_baseline, and --impl reference) times the C oracle, a
 restatement of the reference path pinned to the reference's outputs, with
 OpenMP on all host cores (OMP_PROC_BIND=close, OMP_PLACES=cores), on bounded
@@ -328,13 +335,23 @@ def device_used_bytes() -> int | None:
 def run_ours(args, dist: Dist) -> dict | None:
     from beam_gb300 import WORKLOADS, Graph
 
+    t_start = time.perf_counter()
+
+    def remaining() -> float:
+        """Seconds left of the whole run's time budget (--time-budget-s)."""
+        return args.time_budget_s - (time.perf_counter() - t_start)
+
     spec = WORKLOADS[args.workload]
     t0 = time.perf_counter()
     g = Graph.generate(spec)
     log(f"[bench] graph {args.workload}: n={g.n} m={g.edges} ({time.perf_counter() - t0:.1f}s)")
     device = dist.local_rank
     head_form = args.form
-    others = [] if args.no_other_form else [f for f in FORMS if f != head_form]
+    # the in-process comparison forms; the plain form (thousands of dependent
+    # 64-group blocks, minutes per run) runs last, in a child process bounded
+    # by what is left of the time budget
+    others = [] if args.no_other_form else [f for f in FORMS if f not in (head_form, "plain")]
+    run_plain = not args.no_other_form and head_form != "plain"
     want = golden_hash(args.workload)
 
     # headline form: warm-up, kernel breakdown, timed region
@@ -364,6 +381,8 @@ def run_ours(args, dist: Dist) -> dict | None:
     head_ratio, head_hash = final_metrics(e)
     info = e.ranker_info() if FORMS[head_form].get("ranker") else None
     e.close()
+    log(f"[bench] {head_form}: {args.steps} timed steps, {ms_per_step:.1f} ms per step "
+        f"({time.perf_counter() - t_start:.0f} s into the run)")
     forms = {head_form: {"wall_s_20iter": round(ms_per_step / 1000.0, 4),
                          "merges_per_s": round(value / dist.world, 1),
                          "merges_per_step": t["merges"] // max(1, args.steps),
@@ -376,15 +395,9 @@ def run_ours(args, dist: Dist) -> dict | None:
     # the other forms, for the speed-ups and the cost-ratio comparison
     for other_form in others:
         eo = form_engine(g, device, other_form)
-        if other_form == "plain":
-            # warm-up: the first iteration sizes every buffer
-            eo.divide(1)
-            eo.merge(1, ITERATIONS)
-            o_steps = max(1, args.plain_steps)
-        else:
-            eo.reset()
-            eo.run(ITERATIONS)
-            o_steps = max(1, min(args.steps, 3))
+        eo.reset()
+        eo.run(ITERATIONS)
+        o_steps = max(1, min(args.steps, 3))
         to = timed_steps(eo, o_steps, None)
         o_ms = sum(to["step_ms"]) / o_steps
         o_ratio, o_hash = final_metrics(eo)  # the partition of the last timed run
@@ -398,16 +411,8 @@ def run_ours(args, dist: Dist) -> dict | None:
         if info:
             forms[other_form]["ranker"] = {k: info[k] for k in ("samples", "train_steps", "ranked", "pruned",
                                                                 "train_ms", "final_loss")}
-    if "plain" in forms:
-        forms["plain"]["bit_exact_vs_reference"] = None if want is None else forms["plain"]["partition_hash"] == want
-    comparison = {}
-    if "plain" in forms:
-        for f in forms:
-            if f == "plain":
-                continue
-            comparison[f"speedup_{f}_vs_plain"] = round(forms["plain"]["wall_s_20iter"] / forms[f]["wall_s_20iter"], 3)
-            comparison[f"cost_ratio_delta_abs_{f}_vs_plain"] = round(
-                forms[f]["cost_ratio_mags_compatible"] - forms["plain"]["cost_ratio_mags_compatible"], 6)
+        log(f"[bench] {other_form}: {o_steps} timed steps, {o_ms:.1f} ms per step "
+            f"({time.perf_counter() - t_start:.0f} s into the run)")
 
     # e2e through the C ABI from host buffers: create from the host CSR
     # held in pinned memory (H2D), 20 iterations, partition download (D2H)
@@ -415,6 +420,9 @@ def run_ours(args, dist: Dist) -> dict | None:
     e2e_steps = max(1, min(args.steps, args.e2e_steps))
     e2e_ms, e2e_merges = [], 0
     for i in range(1 + e2e_steps):
+        if i >= 2 and remaining() < 240:
+            e2e_steps = i - 1  # keep the rest of the budget for the CPU baseline and the plain form
+            break
         t1 = time.perf_counter()
         with form_engine(hg, device, head_form) as ee:
             ee.run(ITERATIONS)
@@ -425,6 +433,28 @@ def run_ours(args, dist: Dist) -> dict | None:
             e2e_merges += m
     e2e_max = dist.reduce(sum(e2e_ms), "max")
     e2e_all = dist.reduce(float(e2e_merges), "sum")
+    log(f"[bench] e2e: {e2e_steps} timed steps ({time.perf_counter() - t_start:.0f} s into the run)")
+
+    # the CPU baseline (rank 0, one GPU), then the plain form, both bounded
+    cpu_base = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        cpu_base = cpu_baseline(args, timeout_s=max(60.0, min(300.0, remaining() - 120.0)))
+        log(f"[bench] cpu baseline ({time.perf_counter() - t_start:.0f} s into the run)")
+    if run_plain:
+        forms["plain"] = plain_form(args, device, timeout_s=remaining() - 30.0)
+        log(f"[bench] plain: {forms['plain'].get('wall_s_20iter')} s per 20-iteration run "
+            f"({time.perf_counter() - t_start:.0f} s into the run)")
+        if forms["plain"].get("complete"):
+            forms["plain"]["bit_exact_vs_reference"] = (None if want is None
+                                                        else forms["plain"]["partition_hash"] == want)
+    comparison = {}
+    if forms.get("plain", {}).get("complete"):
+        for f in forms:
+            if f == "plain":
+                continue
+            comparison[f"speedup_{f}_vs_plain"] = round(forms["plain"]["wall_s_20iter"] / forms[f]["wall_s_20iter"], 3)
+            comparison[f"cost_ratio_delta_abs_{f}_vs_plain"] = round(
+                forms[f]["cost_ratio_mags_compatible"] - forms["plain"]["cost_ratio_mags_compatible"], 6)
 
     kernel_ms, kernel_launches = t["kernel_ms"], t["kernel_launches"]
     achieved = t["kernel_bytes"] / (kernel_ms / 1000.0) / 1e9 if kernel_ms > 0 else 0.0
@@ -487,9 +517,10 @@ def run_ours(args, dist: Dist) -> dict | None:
         "breakdown_ms_per_run": breakdown,
         "clocks": clocks.summary(),
         "wall_s_timed_region": round(wall_s, 3),
+        "wall_s_run": round(time.perf_counter() - t_start, 1),
     }
-    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        result["cpu_baseline"] = cpu_baseline(args)
+    if cpu_base is not None:
+        result["cpu_baseline"] = cpu_base
     return result
 
 
@@ -608,18 +639,86 @@ def reexec_with_omp_env() -> None:
     os.execve(sys.executable, [sys.executable, *sys.argv], env)
 
 
-def cpu_baseline(args) -> dict:
+def _text(x) -> str:
+    return x.decode(errors="replace") if isinstance(x, bytes) else (x or "")
+
+
+def cpu_baseline(args, timeout_s: float) -> dict:
     """The oracle on the host cores in a child process (OpenMP placement set
-    before it starts), one bounded sample of the workload."""
+    before it starts), one bounded sample of the workload, stopped after
+    timeout_s."""
     cmd = [sys.executable, str(ROOT / "bench.py"), "--cpu-sample", "--workload", args.workload,
            "--sample-seconds", str(args.cpu_sample_seconds)]
     env = dict(os.environ, **OMP_ENV, OMP_NUM_THREADS=str(os.cpu_count() or 1))
-    proc = subprocess.run(cmd, capture_output=True, text=True, env=env)
-    lines = [l for l in proc.stdout.splitlines() if l.startswith("{")]
-    if proc.returncode != 0 or not lines:
-        return {"value": None, "unit": UNIT, "cores": 0, "kind": "port",
-                "sample": f"CPU sample failed: {proc.stderr[-300:]}"}
+    try:
+        proc = subprocess.run(cmd, capture_output=True, text=True, env=env, timeout=timeout_s)
+        out, err, rc = proc.stdout, proc.stderr, proc.returncode
+    except subprocess.TimeoutExpired as ex:
+        out, err, rc = _text(ex.stdout), _text(ex.stderr), None
+    lines = [l for l in out.splitlines() if l.startswith("{")]
+    if rc != 0 or not lines:
+        why = f"stopped after {timeout_s:.0f} s" if rc is None else f"failed: {err[-300:]}"
+        return {"value": None, "unit": UNIT, "cores": 0, "kind": "port", "sample": f"CPU sample {why}"}
     return json.loads(lines[-1])
+
+
+def plain_form(args, device: int, timeout_s: float) -> dict:
+    """The plain form (the reference's 64-group blocks, bit-exact with the
+    reference) timed in a child process (--plain-child): a warm-up of
+    iteration 1, then one 20-iteration run, its cost ratio and partition hash.
+    The child is stopped when the run's time budget is spent; the form is then
+    reported as incomplete, with the last iteration it finished."""
+    base = {"group_batch_size": FORMS["plain"]["group_batch_size"], "steps": 1}
+    if timeout_s < 60.0:
+        return {**base, "complete": False, "wall_s_20iter": None,
+                "note": "not run: the bench's time budget (--time-budget-s) was spent"}
+    cmd = [sys.executable, str(ROOT / "bench.py"), "--plain-child", "--workload", args.workload,
+           "--plain-device", str(device)]
+    try:
+        proc = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout_s)
+        out, err, rc = proc.stdout, proc.stderr, proc.returncode
+    except subprocess.TimeoutExpired as ex:
+        out, err, rc = _text(ex.stdout), _text(ex.stderr), None
+    lines = [l for l in out.splitlines() if l.startswith("{")]
+    if rc == 0 and lines:
+        return {**json.loads(lines[-1]), **base, "complete": True}
+    progress = [l for l in err.splitlines() if l.startswith("[plain]")]
+    why = (f"stopped at the bench's time budget after {timeout_s:.0f} s" if rc is None
+           else f"child failed (rc {rc}): {err[-300:]}")
+    return {**base, "complete": False, "wall_s_20iter": None, "note": why,
+            "progress": progress[-1] if progress else None}
+
+
+def plain_child(args) -> None:
+    """--plain-child: the plain form's measurement (see plain_form), one JSON
+    line on stdout, progress per iteration on stderr."""
+    from beam_gb300 import WORKLOADS, Graph
+
+    g = Graph.generate(WORKLOADS[args.workload])
+    e = form_engine(g, args.plain_device, "plain")
+    t0 = time.perf_counter()
+    e.divide(1)
+    e.merge(1, ITERATIONS)
+    e.synchronize()
+    warmup_s = time.perf_counter() - t0
+    log(f"[plain] warm-up (iteration 1): {warmup_s:.1f} s")
+    e.reset()
+    e.flush_l2()
+    acc = "accepted_merges_after_validation"
+    m0 = e.stats()[acc]
+    t1 = time.perf_counter()
+    e.step_timer_start()
+    for it in range(1, ITERATIONS + 1):
+        e.divide(it)
+        e.merge(it, ITERATIONS)
+        log(f"[plain] iteration {it} of {ITERATIONS} done, {time.perf_counter() - t1:.1f} s into the timed run")
+    ms = e.step_timer_stop()
+    merges = e.stats()[acc] - m0
+    ratio, phash = final_metrics(e)
+    e.close()
+    print(json.dumps({"wall_s_20iter": round(ms / 1000.0, 4), "merges_per_s": round(merges / (ms / 1000.0), 1),
+                      "merges_per_step": merges, "cost_ratio_mags_compatible": round(ratio, 6),
+                      "partition_hash": phash, "warmup_s": round(warmup_s, 1)}), flush=True)
 
 
 def cpu_sample_main(args) -> None:
@@ -691,7 +790,11 @@ def main():
     ap.add_argument("--form", choices=list(FORMS), default="ranker",
                     help="form whose throughput is the headline value")
     ap.add_argument("--no-other-form", action="store_true", help="skip timing the other forms")
-    ap.add_argument("--plain-steps", type=int, default=1, help="timed runs of the plain form")
+    ap.add_argument("--time-budget-s", type=float, default=1380.0,
+                    help="wall budget of the whole run: the CPU baseline and the plain form (run last) are "
+                         "stopped when it is spent")
+    ap.add_argument("--plain-child", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--plain-device", type=int, default=0, help=argparse.SUPPRESS)
     ap.add_argument("--e2e-steps", type=int, default=5, help="timed e2e runs (at most --steps)")
     ap.add_argument("--batch-groups", type=int, default=None,
                     help="groups per block of the batched and ranker forms (default: all groups of an iteration)")
@@ -710,6 +813,9 @@ def main():
         return
     if args.cpu_sample:
         cpu_sample_main(args)
+        return
+    if args.plain_child:
+        plain_child(args)
         return
     if args.warmup < 3:
         args.warmup = 3
