@@ -45,3 +45,31 @@ def test_ncu_commands_keep_clocks():
         assert cmds, p.name
         for c in cmds:
             assert "--clock-control none" in c, (p.name, c)
+
+
+def test_plain_form_is_bounded():
+    """The plain form runs in a child process bounded by the bench's time
+    budget: with no budget left it is not started, and a child that cannot
+    finish (here: no GPU in the process, or a GPU run) is reported with
+    `complete` set accordingly, never as a 20-iteration time it did not
+    measure."""
+    import types
+    sys.path.insert(0, str(ROOT))
+    import bench
+    args = types.SimpleNamespace(workload="dcsbm_4096")
+    r = bench.plain_form(args, 0, 30.0)
+    assert r["complete"] is False and r["wall_s_20iter"] is None and "time budget" in r["note"]
+    r = bench.plain_form(args, 0, 300.0)
+    if r["complete"]:
+        assert r["wall_s_20iter"] > 0 and r["partition_hash"]
+    else:
+        assert r["wall_s_20iter"] is None and r["note"]
+
+
+def test_cpu_baseline_is_bounded():
+    import types
+    sys.path.insert(0, str(ROOT))
+    import bench
+    args = types.SimpleNamespace(workload="dcsbm_4096", cpu_sample_seconds=0.5)
+    r = bench.cpu_baseline(args, timeout_s=0.01)
+    assert r["value"] is None and "stopped after" in r["sample"]
