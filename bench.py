@@ -685,6 +685,7 @@ def plain_form(args, device: int, timeout_s: float) -> dict:
     progress = [l for l in err.splitlines() if l.startswith("[plain]")]
     why = (f"stopped at the bench's time budget after {timeout_s:.0f} s" if rc is None
            else f"child failed (rc {rc}): {err[-300:]}")
+    log(f"[bench] plain form incomplete: {why}; last progress: {progress[-1] if progress else 'none'}")
     return {**base, "complete": False, "wall_s_20iter": None, "note": why,
             "progress": progress[-1] if progress else None}
 
@@ -696,6 +697,7 @@ def plain_child(args) -> None:
 
     g = Graph.generate(WORKLOADS[args.workload])
     e = form_engine(g, args.plain_device, "plain")
+    log("[plain] engine ready, warm-up (iteration 1) started")
     t0 = time.perf_counter()
     e.divide(1)
     e.merge(1, ITERATIONS)
