@@ -700,6 +700,8 @@ def plain_child(args) -> None:
     log("[plain] engine ready, warm-up (iteration 1) started")
     t0 = time.perf_counter()
     e.divide(1)
+    e.synchronize()
+    log(f"[plain] warm-up Divide: {time.perf_counter() - t0:.1f} s")
     e.merge(1, ITERATIONS)
     e.synchronize()
     warmup_s = time.perf_counter() - t0
