@@ -173,13 +173,14 @@ __global__ void __launch_bounds__(256) MinHashKernel(const int* __restrict__ arc
                                                      unsigned long long* __restrict__ hash,
                                                      unsigned long long* __restrict__ stats) {
   const long long total = arcs + n;
-  // algorithmic bytes of one dimension: per arc its source, target, the
-  // source's label and its need stamp (16 B); per node its label and stamp
-  // and the supernode's hash word (16 B)
+  // algorithmic bytes of one dimension: per arc its source, the source's
+  // label and its need stamp (12 B), per node its label and stamp (8 B), and
+  // the target of every arc that is hashed (4 B, counted per warp below)
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    atomicAdd(&stats[kStDivideBytes], 16ull * static_cast<unsigned long long>(arcs) +
-                                          16ull * static_cast<unsigned long long>(n));
+    atomicAdd(&stats[kStDivideBytes], 12ull * static_cast<unsigned long long>(arcs) +
+                                          8ull * static_cast<unsigned long long>(n));
   }
+  unsigned hashed_arcs = 0;  // warp-uniform; a warp's share of one launch stays far below 2^32
   const int lane = threadIdx.x & 31;
   const long long warp = (static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = (static_cast<long long>(gridDim.x) * blockDim.x) >> 5;
@@ -202,6 +203,7 @@ __global__ void __launch_bounds__(256) MinHashKernel(const int* __restrict__ arc
     for (int u = 0; u < kHashUnroll; ++u) {
       const long long t = t0 + 32 * u + lane;
       x[u] = rep[u] < 0 ? 0 : t < arcs ? col[t] : node[u];
+      hashed_arcs += __popc(__ballot_sync(0xffffffffu, rep[u] >= 0 && t < arcs));
     }
 #pragma unroll
     for (int u = 0; u < kHashUnroll; ++u) {
@@ -219,6 +221,7 @@ __global__ void __launch_bounds__(256) MinHashKernel(const int* __restrict__ arc
       if (rep[u] >= 0 && lane == leader) atomicMin(&hash[rep[u]], g);
     }
   }
+  if (lane == 0 && hashed_arcs) atomicAdd(&stats[kStDivideBytes], 4ull * static_cast<unsigned long long>(hashed_arcs));
 }
 
 __global__ void GatherKeysKernel(const int* __restrict__ order, const int* __restrict__ pos_map, int items,
